@@ -1,0 +1,86 @@
+"""The FP64 oracle against golden vectors produced by the reference's own
+source files (``tests/golden/make_golden.py``)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pf_oracle as O
+
+G = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _load(name):
+    return np.load(os.path.join(G, name))
+
+
+def _args(d):
+    keys = ("dim", "T_liquidus", "gas_const", "Qg", "L0", "kappa_g", "m_g", "ad_hoc")
+    a = dict(zip(keys, d["pf_keys"].tolist()))
+    a.update(Nx=int(d["Nx"]), Ny=int(d["Ny"]), Nz=int(d["Nz"]), num_oris=int(d["n"]),
+             anisotropy=float(d["anisotropy"]), h=tuple(d["h"].tolist()))
+    return a
+
+
+@pytest.mark.parametrize("name", ["pf_iso.npz", "pf_aniso.npz", "pf_aniso_n20.npz"])
+def test_pf_steps_match_reference(name):
+    d = _load(name)
+    a = _args(d)
+    eta = d["eta_in"]
+    dt = float(d["dt"])
+    t = 0.0
+    for k in range(int(d["steps"])):
+        eta = O.explicit_euler(eta, t, t + dt, d["T"], a, d["grain_dirs"])
+        t += dt
+        np.testing.assert_allclose(eta, d["eta_out"][k], rtol=1e-12, atol=1e-14)
+
+
+def test_ini_cond_matches_reference():
+    d = _load("pf_aniso.npz")
+    np.testing.assert_array_equal(O.ini_cond(d["cell_ori_inds"], int(d["n"])), d["eta_ini"])
+
+
+def test_force_and_inspect_match_reference():
+    d = _load("pf_force_inspect.npz")
+    np.testing.assert_array_equal(O.force_liquid_zero(d["eta"], d["T"], 1623.0, 1.0),
+                                  d["eta_forced"])
+    m = O.inspect(d["eta"], d["eta0"], d["T"], 1623.0)
+    np.testing.assert_allclose([m["pct_ori_changed"], m["pct_liquid"], m["max_T"]],
+                               d["inspect"], rtol=1e-12)
+
+
+def _gamma(d):
+    keys = ("eta", "r", "rho", "h", "eps", "SB", "T0", "Ts", "Tl", "L")
+    return dict(zip(keys, d["gamma"].tolist()))
+
+
+@pytest.mark.parametrize("name,dtype,rtol", [("heat_f64.npz", np.float64, 1e-13),
+                                             ("heat_f32.npz", np.float32, 2e-6)])
+def test_heat_matches_reference(name, dtype, rtol):
+    d = _load(name)
+    g = _gamma(d)
+    dx, dy, dz, dt = d["dxyzt"].tolist()
+    T = d["T_in"].astype(np.float64)
+    nx, ny = T.shape[0] - 2, T.shape[1] - 2
+    xt, yt = O.cell_centres_top(nx, ny, dx, dy)
+    for k, (xl, yl, P) in enumerate(d["lasers"]):
+        T = O.heat_update_T(T, xl, yl, xt, yt, P, dx, dy, dz, dt, g)
+        np.testing.assert_allclose(T, d["T_out"][k], rtol=rtol)
+
+
+def test_tsources_match_reference():
+    d = _load("tsources.npz")
+    c, t = d["centroids"], float(d["t"])
+    np.testing.assert_allclose(O.T_quench(c, t, 1623.0), d["T_quench"], rtol=1e-13)
+    np.testing.assert_allclose(
+        O.T_rosenthal(c, t, 300.0, x0=0.2e-3, vel=0.6e-3 / 2.4e-3, y_c=1.2e-4, z_top=1e-4),
+        d["T_rosenthal"], rtol=1e-12)
+    ts, xs, ys, zs, ps, dirs = O.read_path([0.1e-3, 0.9e-3, 0.9e-3, 0.1e-3],
+                                           [0.17e-3, 0.17e-3, 0.07e-3, 0.07e-3],
+                                           [0.1e-3] * 4, [1, 1, 1, 0], 0.25, 2e-7)
+    for a, b in ((ts, "path_ts"), (xs, "path_xs"), (ys, "path_ys"), (zs, "path_zs"),
+                 (ps, "path_ps"), (dirs, "path_dirs")):
+        np.testing.assert_allclose(a, d[b], rtol=1e-13)
+    i = int(d["path_i"])
+    np.testing.assert_allclose(
+        O.T_rosenthal_path(c, 300.0, 0.25, xs[i], ys[i], zs[i], dirs[i]), d["T_path"], rtol=1e-12)
