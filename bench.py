@@ -1,0 +1,345 @@
+"""Benchmark of the fused heat + phase-field step on GB300.
+
+Workload (default): single-track laser scan, 400 x 200 x 100 cells (8M) at
+h = 1 um, Voronoi polycrystal of 2000 grains with 20 orientations, cubic
+anisotropy 0.15, explicit FD heat equation with a Gaussian surface source
+(200 W, r = 50 um, absorptivity 0.4, 0.8 m/s along x, T0 = 300 K),
+Arrhenius mobility, float32.  A "step" is one fused heat + phase-field update
+of the whole grid; the default K = 2000 steps is the workload's full run.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Rank 0 prints one JSON line.  Under torchrun each rank runs its own replica
+(the path does not shard on one box: "replicas only"), value sums over ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+WORKLOAD = dict(name="laser_track_8M", Nx=400, Ny=200, Nz=100, h=1e-6, num_grains=2000,
+                num_oris=20, anisotropy=0.15, power=200.0, radius=5e-5, absorptivity=0.4,
+                speed=0.8, T0=300.0, T_liquidus=1623.0, seed=2)
+PF_KEYS = dict(T_liquidus=1623.0, gas_const=8.3, Qg=1.4e5, L0=3.5e3, kappa_g=2.77e-6, m_g=2.4e5,
+               ad_hoc=1.0)
+METRIC = "cell_orientation_updates_per_s"
+UNIT = "cell*ori/s"
+KERNEL = "pf_zmarch_kernel<4, true, 1> (fused heat + anisotropic phase field)"
+
+
+def gamma_args(w):
+    g = dict(eta=w["absorptivity"], r=w["radius"], rho=8440.0, h=10.0, eps=0.4, SB=5.67e-8,
+             T0=w["T0"], Ts=1563.0, Tl=1623.0)
+    g["L"] = 290e3 / (g["Tl"] - g["Ts"])
+    return g
+
+
+def algorithmic_bytes_per_step(w):
+    """Read eta + write eta + read T + write T, float32 (padding and halo
+    re-reads excluded): N (2 n 4 + 2 4)."""
+    N = w["Nx"] * w["Ny"] * w["Nz"]
+    return N * (2 * w["num_oris"] * 4 + 8)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes per launch of the top kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "pf_zmarch_laser_track_8M.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def build_case(w, device_run=True):
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    from jax_am_gb300.phase_field.utils import Field
+    from jax_am_gb300.runner import HeatPFRun, single_track
+    pf_args = dict(PF_KEYS, Nx=w["Nx"], Ny=w["Ny"], Nz=w["Nz"], h=w["h"],
+                   num_grains=w["num_grains"], num_oris=w["num_oris"], anisotropy=w["anisotropy"],
+                   T_liquidus=w["T_liquidus"])
+    poly = Field(pf_args, seed=w["seed"])
+    solver = PFSolver(pf_args, poly)
+    g = gamma_args(w)
+    path = single_track(50e-6, 0.5 * w["Ny"] * w["h"], w["speed"], w["power"], 1.0)
+    return solver, g, path, poly
+
+
+def time_cpu_baseline(w, budget_s=15.0, threads=None, sample=(100, 50, 25), steps_max=50):
+    """The float32 PyTorch restatement of the same fused step on the host
+    cores, on a reduced grid (bounded sample), in cell*ori updates/s."""
+    from oracle import pf_torch as PT
+    from jax_am_gb300.phase_field.utils import grain_directions, random_quaternions
+    threads = threads or os.cpu_count()
+    torch.set_num_threads(threads)
+    nx, ny, nz = sample
+    n = w["num_oris"]
+    rng = np.random.default_rng(0)
+    a = dict(PF_KEYS, anisotropy=w["anisotropy"], h=(w["h"],) * 3)
+    dirs = torch.tensor(grain_directions(random_quaternions(n, rng)), dtype=torch.float32)
+    inds = rng.integers(0, n, nx * ny * nz)
+    eta = torch.zeros((nz * ny * nx, n))
+    eta[torch.arange(nz * ny * nx), torch.tensor(inds)] = 1.0
+    eta = eta.reshape(nz, ny, nx, n)
+    Tg = torch.full((nz + 2, ny + 2, nx + 2), w["T0"])
+    g = gamma_args(w)
+    dt = 3e-8
+
+    def laser(t):
+        return 20e-6 + w["speed"] * t, 0.5 * ny * w["h"], w["power"]
+
+    with torch.no_grad():
+        PT.coupled_step(eta, Tg, 0.0, dt, a, g, laser, dirs)  # warm-up
+        t0 = time.perf_counter()
+        steps = 0
+        while steps < steps_max and (time.perf_counter() - t0) < budget_s:
+            eta, Tg = PT.coupled_step(eta, Tg, steps * dt, dt, a, g, laser, dirs)
+            steps += 1
+        el = time.perf_counter() - t0
+    value = nx * ny * nz * n * steps / el
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} fused steps of the float32 PyTorch-CPU restatement "
+                      f"(oracle/pf_torch.py) on {nx}x{ny}x{nz} cells, n={n}, A={w['anisotropy']}, "
+                      f"{el:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    cb = time_cpu_baseline(WORKLOAD, budget_s=max(5.0, 2.0 * args.steps), steps_max=10 ** 6)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": WORKLOAD["name"], "cells": "100x50x25 sample",
+                                        "num_oris": WORKLOAD["num_oris"]},
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "JAX (the reference's runtime) is not installable here; the reference arm times "
+                "the PyTorch-CPU restatement of the reference algorithm on all host threads",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import __graft_entry__
+    __graft_entry__.build()
+    from jax_am_gb300.runner import HeatPFRun
+
+    w = WORKLOAD
+    solver, g, path, poly = build_case(w)
+    N = w["Nx"] * w["Ny"] * w["Nz"]
+    n = w["num_oris"]
+    run = HeatPFRun(solver, g, path)
+    run.run(args.warmup, graph=True)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    stream = torch.cuda.current_stream()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    launches0 = run.launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    run.run(args.steps, graph=True)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    gpu_launches = run.launches - launches0
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = N * n * args.steps * world / (ms / 1e3)
+
+    # roofline of the fused kernel: one launch per step
+    bytes_step = algorithmic_bytes_per_step(w)
+    peak, peak_kind = measured_peak()
+    achieved = bytes_step / (ms_per_step / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic_per_launch(),
+                "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind ==
+                "measured" else "fallback 6.8 TB/s", "kernel": KERNEL,
+                "algorithmic_bytes_per_launch": bytes_step}
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = time_e2e(solver, g, path, w, args.steps)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = time_cpu_baseline(w)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": w["name"], "grid": [w["Nx"], w["Ny"], w["Nz"]],
+                       "num_oris": n, "num_grains": w["num_grains"],
+                       "anisotropy": w["anisotropy"], "dt": run.dt,
+                       "heat": "fused explicit FD + Gaussian 200 W", "parallelism": "replicas",
+                       "l2": "inputs larger than L2 (eta 640 MB per buffer)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": gpu_launches, "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def time_e2e(solver, g, path, w, steps):
+    """The same K-step solve through the public API starting from host
+    memory: the initial eta and T are copied from pinned host buffers, the
+    run steps on the device with the reference's inspect_sol cadence (every
+    20 steps a metrics record is read back to the host), and the final eta
+    and T are copied back.  Bytes per step are the totals divided by K."""
+    from jax_am_gb300.runner import HeatPFRun
+    N = w["Nx"] * w["Ny"] * w["Nz"]
+    n = w["num_oris"]
+    eta_h = solver.ini_cond().cpu().pin_memory()
+    T_h = torch.full((w["Nz"] + 2, w["Ny"] + 2, w["Nx"] + 2), w["T0"]).pin_memory()
+    eta_out = torch.empty_like(eta_h).pin_memory()
+    T_out = torch.empty_like(T_h).pin_memory()
+    check_every = 20
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eta_d = eta_h.to("cuda", non_blocking=True)
+    T_d = T_h.to("cuda", non_blocking=True)
+    run = HeatPFRun(solver, g, path, eta0=eta_d, T_init=T_d)
+    d2h_diag = 0
+    done = 0
+    while done < steps:
+        k = min(check_every, steps - done)
+        run.run(k, graph=(k == check_every))
+        done += k
+        d = solver.diagnostics(run.state, run.T_ghosted, T_ghosted=True)
+        d2h_diag += 8 * (6 + 64)
+        if d["n_nonfinite"]:
+            raise ValueError("non-finite eta")
+    eta_out.copy_(run.state, non_blocking=True)
+    T_out.copy_(run.T_ghosted, non_blocking=True)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    h2d = eta_h.numel() * 4 + T_h.numel() * 4
+    d2h = eta_out.numel() * 4 + T_out.numel() * 4 + d2h_diag
+    return {"value": N * n * steps / el, "unit": UNIT, "h2d_bytes_per_step": h2d / steps,
+            "d2h_bytes_per_step": d2h / steps, "seconds": el,
+            "path": "HeatPFRun (public API) + PFSolver.diagnostics every 20 steps, "
+                    "state uploaded from and returned to pinned host memory"}
+
+
+if __name__ == "__main__":
+    main()

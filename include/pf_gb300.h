@@ -1,0 +1,212 @@
+/*
+ * pf_gb300.h -- C ABI of the GB300 (sm_103a) phase-field grain-growth library.
+ *
+ * The library advances JAX-AM's multi-order-parameter Allen-Cahn grain-growth
+ * model (jax_am/phase_field/allen_cahn.py) and its explicit finite-difference
+ * heat equation with a moving Gaussian laser (jax_am/cfd/gamma.py) on one GPU.
+ *
+ * Conventions shared by every entry point:
+ *  - All array arguments are DEVICE pointers owned by the caller.  Nothing is
+ *    allocated inside the library unless an entry point says so.
+ *  - eta is float32, shape (nz, ny, nx, num_oris), C order: x fastest among
+ *    the cells, orientation innermost -- the reference's (N, num_oris) array
+ *    with cells in z-major order (allen_cahn.py:60, phase_field/utils.py:188).
+ *  - A per-cell temperature T is float32 (nz, ny, nx) -- the reference's
+ *    (N, 1) ode_params array.
+ *  - The heat state Tg is float32 (nz+2, ny+2, nx+2) with one ghost layer,
+ *    x fastest.  The reference holds the same ghosted field as
+ *    (nx+2, ny+2, nz+2), x slowest (applications/cfd/gamma/example.py:85);
+ *    the Python layer transposes at the boundary.  Ghost faces are part of
+ *    the state: each step reads the previous ghosts and writes new ones
+ *    (gamma.py:23-42).  Edge and corner ghosts are never read or written.
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy
+ *    default stream.  Work is enqueued on it and the call returns without
+ *    synchronising.
+ *  - The return value is 0 (PFG_OK) or a pfg_status code; no exception ever
+ *    crosses the ABI.  pfg_status_string() names a code.
+ *  - input and output buffers of one step must not overlap.
+ */
+#ifndef PF_GB300_H
+#define PF_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PFG_ABI_VERSION 1
+#define PFG_MAX_ORIS 64      /* orientations per cell */
+#define PFG_MAX_SEGMENTS 16  /* laser tool-path segments */
+
+typedef enum pfg_status {
+  PFG_OK = 0,
+  PFG_ERR_SHAPE = 1,        /* a grid extent < 1, or num_oris outside [1, PFG_MAX_ORIS] */
+  PFG_ERR_NULL = 2,         /* a required pointer is NULL */
+  PFG_ERR_ALIGN = 3,        /* a device pointer is not 16-byte aligned */
+  PFG_ERR_PARAM = 4,        /* a parameter is out of its domain (h <= 0, bad bc code, ...) */
+  PFG_ERR_LAUNCH = 5,       /* the CUDA launch failed; see pfg_last_cuda_error() */
+  PFG_ERR_TIMEOUT = 6,      /* a bounded device-side wait ran out */
+  PFG_ERR_CAPACITY = 7,     /* a job table or scratch buffer is too small */
+  PFG_ERR_NO_DEVICE = 8     /* no usable sm_103 device */
+} pfg_status;
+
+typedef enum pfg_bc { PFG_BC_NEUMANN = 0, PFG_BC_PERIODIC = 1 } pfg_bc;
+
+typedef enum pfg_layout { PFG_LAYOUT_ZYX = 0, PFG_LAYOUT_XYZ = 1 } pfg_layout;
+
+/* Phase-field parameters: the reference pf_args keys (pf_params.yaml) plus the
+ * polycrystal's cell size and grain directions (phase_field/utils.py:55-62,
+ * 104-109). */
+typedef struct pfg_pf_params {
+  int32_t nx, ny, nz;      /* cells along x, y, z (pf_args Nx, Ny, Nz) */
+  int32_t num_oris;        /* orientations per cell (pf_args num_oris) */
+  float h_x, h_y, h_z;     /* cell size [m] (Field.mesh_h_xyz) */
+  float T_liquidus;        /* [K] */
+  float gas_const;         /* [J/(mol K)] */
+  float Qg;                /* [J/mol] */
+  float L0;                /* [m^3/(J s)] */
+  float kappa_g;           /* [J/m] */
+  float m_g;               /* [J/m^3] */
+  float anisotropy;        /* 0 disables the anisotropy term, as the reference does */
+  float ad_hoc;
+  int32_t bc_x, bc_y, bc_z;   /* pfg_bc per axis; the reference is Neumann on all faces */
+  int32_t force_liquid_zero;  /* 1: eta = 0 where T > T_liquidus + liquid_shift after the
+                                 step (allen_cahn.py:117-128; off in the reference stepper) */
+  float liquid_shift;         /* [K], 1.0 in the reference */
+  float grain_dirs[3 * PFG_MAX_ORIS * 3];  /* (3, num_oris, 3): rotated cube axes */
+} pfg_pf_params;
+
+/* One straight tool-path segment: between times t0 and t1 the beam moves
+ * linearly from (x0, y0) to (x1, y1) at `power` watts.  Outside every
+ * segment the beam is off. */
+typedef struct pfg_segment {
+  float t0, t1, x0, y0, x1, y1, power, reserved;
+} pfg_segment;
+
+/* Heat-equation parameters: the reference gamma_args dict
+ * (applications/cfd/gamma/example.py:67-79) plus the grid. */
+typedef struct pfg_heat_params {
+  int32_t nx, ny, nz;      /* interior cells */
+  float dx, dy, dz;        /* [m] */
+  float rho;               /* density (gamma_args rho) */
+  float h_conv;            /* convection coefficient (gamma_args h) */
+  float emissivity;        /* (gamma_args eps) */
+  float sigma_sb;          /* Stefan-Boltzmann constant (gamma_args SB) */
+  float T0;                /* ambient temperature (gamma_args T0) */
+  float Ts, Tl;            /* solidus / liquidus (gamma_args Ts, Tl) */
+  float latent;            /* latent heat per kelvin of mushy range (gamma_args L) */
+  float absorptivity;      /* (gamma_args eta) */
+  float beam_radius;       /* (gamma_args r) */
+  float x_first, y_first;  /* centre of the first cell along x and y (dx/2, dy/2 in the
+                              reference driver, applications/cfd/gamma/example.py:61-62) */
+  int32_t layout;          /* PFG_LAYOUT_ZYX: Tg is (nz+2, ny+2, nx+2), x fastest (required by
+                              pfg_heat_pf_step); PFG_LAYOUT_XYZ: the reference's (nx+2, ny+2,
+                              nz+2), z fastest (accepted by pfg_heat_step) */
+  int32_t num_segments;    /* tool path used by pfg_heat_pf_step; 0..PFG_MAX_SEGMENTS */
+  pfg_segment path[PFG_MAX_SEGMENTS];
+} pfg_heat_params;
+
+/* Simulation clock kept on the device so that a captured CUDA graph of fused
+ * steps advances time without the host. */
+typedef struct pfg_clock {
+  double t;       /* time at the start of the step [s] */
+  int64_t step;   /* steps taken */
+} pfg_clock;
+
+/* Moving linear temperature gradient of the directional-solidification
+ * driver (applications/phase_field/solidification/example.py:21-34):
+ *   T(z, t) = T_base + grad * (z - z0) - grad * vel * t
+ * with z the cell-centre height z_first + iz * h_z.  The reference has
+ * z0 = 0 and T_base = T_liquidus. */
+typedef struct pfg_quench {
+  double T_base;   /* [K] */
+  double grad;     /* [K/m] */
+  double vel;      /* [m/s] */
+  double z0;       /* [m] */
+  double z_first;  /* centre of the first cell along z [m] */
+} pfg_quench;
+
+/* Results of pfg_pf_diag (device memory, written by the call). */
+typedef struct pfg_diag {
+  double energy;                 /* total free energy [J], float64 accumulation */
+  double max_T;                  /* max over cells of T */
+  int64_t n_cells;
+  int64_t n_ori_changed;         /* cells whose argmax orientation differs from argmax0 */
+  int64_t n_liquid;              /* cells with T >= T_liquidus */
+  int64_t n_nonfinite;           /* eta entries that are NaN or Inf */
+  double mass[PFG_MAX_ORIS];     /* sum over cells of eta_i, float64 accumulation */
+} pfg_diag;
+
+/* ---- library information ----------------------------------------------- */
+int pfg_abi_version(void);
+const char* pfg_status_string(int status);
+/* The last CUDA error string seen by an entry point on this thread. */
+const char* pfg_last_cuda_error(void);
+/* sizeof() of the ABI structs, so bindings can check their mirrors:
+ * 0 pfg_pf_params, 1 pfg_segment, 2 pfg_heat_params, 3 pfg_clock, 4 pfg_diag,
+ * 5 pfg_quench. */
+int64_t pfg_struct_size(int which);
+
+/* ---- phase field --------------------------------------------------------
+ * One explicit Euler step of the Allen-Cahn grain-growth model with the
+ * temperature held at T (the start-of-step value):
+ *   eta_out = eta_in + dt * rhs(eta_in, T).
+ * Replaces explicit_euler + state_rhs (allen_cahn.py:53-85, 106-114) as
+ * called by PFSolver.stepper (allen_cahn.py:139-143).  T is (nz, ny, nx). */
+int pfg_pf_step(const pfg_pf_params* p, const float* eta_in, float* eta_out,
+                const float* T, float dt, void* stream);
+
+/* The same step with T taken from the moving gradient q at the start-of-step
+ * time clk_in->t (the solidification driver refreshes T after each step,
+ * solidification/example.py:84-86), evaluated per z plane inside the kernel
+ * so no temperature array is read.  Writes clk_out = {t + dt, step + 1};
+ * clk_out must not alias clk_in. */
+int pfg_pf_step_quench(const pfg_pf_params* p, const pfg_quench* q, const float* eta_in,
+                       float* eta_out, const pfg_clock* clk_in, pfg_clock* clk_out, float dt,
+                       void* stream);
+
+/* ---- heat ----------------------------------------------------------------
+ * One explicit heat step on the ghosted field, beam at (xl, yl) with the
+ * given power.  Replaces gamma.update_T (gamma.py:55-61).  Tg_in and Tg_out
+ * are ghosted in h->layout (either order); interior cells and the six ghost
+ * faces of Tg_out are written, edge/corner ghosts are left untouched. */
+int pfg_heat_step(const pfg_heat_params* h, const float* Tg_in, float* Tg_out,
+                  float xl, float yl, float power, float dt, void* stream);
+
+/* ---- fused heat + phase field -------------------------------------------
+ * One pass that reads eta and the ghosted temperature and writes both:
+ *   eta_out = eta_in + dt * rhs(eta_in, T_in interior)     (phase field at the
+ *             start-of-step temperature, as the reference drivers do)
+ *   Tg_out  = update_T(Tg_in) with the beam taken from h->path at the
+ *             mid-step time clk_in->t + dt/2.
+ * The clock is read from clk_in and clk_out = {t + dt, step + 1} is written,
+ * so alternating (in, out) buffers inside a CUDA graph advance time on the
+ * device.  The grids of p and h must agree. */
+int pfg_heat_pf_step(const pfg_pf_params* p, const pfg_heat_params* h,
+                     const float* eta_in, float* eta_out,
+                     const float* Tg_in, float* Tg_out,
+                     const pfg_clock* clk_in, pfg_clock* clk_out,
+                     float dt, void* stream);
+
+/* ---- diagnostics ----------------------------------------------------------
+ * The metrics PFSolver.inspect_sol prints (allen_cahn.py:165-180) plus the
+ * float64 free energy and per-orientation mass, reduced on the device.
+ *  T:         per-cell (nz, ny, nx) when T_ghosted == 0, else the ghosted
+ *             (nz+2, ny+2, nx+2) heat state.
+ *  argmax0:   (nz, ny, nx) int32 reference orientation map, or NULL (then
+ *             n_ori_changed is 0).
+ *  argmax_out:(nz, ny, nx) int32 argmax orientation per cell (first maximum,
+ *             all-zero cells give 0, as np.argmax), or NULL.
+ *  scratch:   device buffer of at least pfg_pf_diag_scratch_bytes(p) bytes.
+ *  out:       device pointer to one pfg_diag. */
+int64_t pfg_pf_diag_scratch_bytes(const pfg_pf_params* p);
+int pfg_pf_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_ghosted,
+                const int32_t* argmax0, int32_t* argmax_out,
+                void* scratch, int64_t scratch_bytes, pfg_diag* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PF_GB300_H */

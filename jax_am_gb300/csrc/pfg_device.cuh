@@ -1,0 +1,250 @@
+// Device-side helpers shared by the phase-field, heat, diagnostics, batch and
+// adjoint kernels.  Internal to the library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pf_gb300.h"
+
+namespace pfg {
+
+constexpr int kThreads = 256;  // threads per CTA of every stencil kernel
+
+// ---------------------------------------------------------------------------
+// cp.async (LDGSTS) wrappers: global -> shared copies that bypass registers.
+// ---------------------------------------------------------------------------
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  if constexpr (BYTES == 16) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+  } else if constexpr (BYTES == 8) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem));
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem));
+  }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait(int pending) {
+  // wait_group takes an immediate
+  if (pending <= 0) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  else if (pending == 1) asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+  else asm volatile("cp.async.wait_group 2;\n" ::: "memory");
+}
+
+// Vector of V floats moved as one 4/8/16-byte access.
+template <int V>
+struct VecF {
+  float v[V];
+  __device__ __forceinline__ void load(const float* p) {
+    if constexpr (V == 4) {
+      const float4 t = *reinterpret_cast<const float4*>(p);
+      v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    } else if constexpr (V == 2) {
+      const float2 t = *reinterpret_cast<const float2*>(p);
+      v[0] = t.x; v[1] = t.y;
+    } else {
+      v[0] = *p;
+    }
+  }
+  __device__ __forceinline__ void store(float* p) const {
+    if constexpr (V == 4) {
+      *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else if constexpr (V == 2) {
+      *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+    } else {
+      *p = v[0];
+    }
+  }
+  __device__ __forceinline__ void store_stream(float* p) const {
+    if constexpr (V == 4) {
+      __stcs(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
+    } else if constexpr (V == 2) {
+      __stcs(reinterpret_cast<float2*>(p), make_float2(v[0], v[1]));
+    } else {
+      __stcs(p, v[0]);
+    }
+  }
+};
+
+// Index of a neighbour plane/row/column under the boundary condition:
+// Neumann replicates the edge cell (allen_cahn.py:61-66), periodic wraps.
+__device__ __forceinline__ int bc_index(int i, int n, int periodic) {
+  if (i < 0) return periodic ? i + n : 0;
+  if (i >= n) return periodic ? i - n : n - 1;
+  return i;
+}
+
+// ---------------------------------------------------------------------------
+// Phase-field per-cell constants.
+// With S = sum_j eta_j^2 and gamma = 1 (allen_cahn.py:43) the energy gradient
+// m_g [eta^3 - eta + 4 eta (S - eta^2) + 2 (1 - zeta)^2 eta] / ad_hoc
+// (allen_cahn.py:42-51,58) equals (m_g/ad_hoc) eta (K - 3 eta^2) with
+// K = 4 S + 2 (1 - zeta)^2 - 1, and one Euler step is
+//   eta' = eta + cg * eta (K - 3 eta^2) + cl * a * Lap(eta),
+//   cg = -dt Lg m_g / ad_hoc,   cl = dt Lg kappa_g ad_hoc,
+// where Lap sums (eta_+ - eta) + (eta_- - eta) over axes weighted by 1/h^2.
+// ---------------------------------------------------------------------------
+struct PFConsts {
+  float wx, wy, wz;          // 1/h^2 per axis
+  float T_liq, inv_T_liq;    // liquidus
+  float neg_Qg_over_R;       // -Qg / gas_const
+  float L0;
+  float mg_ad;               // m_g / ad_hoc
+  float kappa_ad;            // kappa_g * ad_hoc
+  float aniso;               // anisotropy strength A
+  float liquid_limit;        // T_liquidus + liquid_shift
+  int force;                 // liquid forcing on/off
+};
+
+struct CellCoef {
+  float cg, cl, K, liquid;  // liquid: 1.0 when forcing zeroes this cell
+};
+
+// The temperature-only part of a cell's coefficients.
+struct TempCoef {
+  float cg, cl;   // see above
+  float om2;      // 2 (1 - zeta)^2
+  float liquid;   // 1.0 when liquid forcing zeroes the cell
+};
+
+__device__ __forceinline__ TempCoef temp_coefficients(const PFConsts& c, float T, float dt) {
+  // T > 2000 is clipped (allen_cahn.py:56); written as a select so that NaN passes through
+  const float Tc = (T > 2000.f) ? 2000.f : T;
+  const float zeta = 0.5f * (1.f - tanhf(1e10f * (Tc / c.T_liq - 1.f)));  // allen_cahn.py:57
+  const float Lg = c.L0 * expf(c.neg_Qg_over_R / Tc);                      // allen_cahn.py:83
+  const float om = 1.f - zeta;
+  TempCoef r;
+  r.cg = -dt * Lg * c.mg_ad;
+  r.cl = dt * Lg * c.kappa_ad;
+  r.om2 = 2.f * om * om;
+  // forcing compares the unclipped start-of-step T (allen_cahn.py:124-126)
+  r.liquid = (c.force && T > c.liquid_limit) ? 1.f : 0.f;
+  return r;
+}
+
+__device__ __forceinline__ CellCoef cell_coefficients(const TempCoef& t, float S) {
+  CellCoef r;
+  r.cg = t.cg;
+  r.cl = t.cl;
+  r.K = 4.f * S + t.om2 - 1.f;
+  r.liquid = t.liquid;
+  return r;
+}
+
+// Cubic anisotropy factor 1 + A (cos^4 t + sin^4 t) where t is the smallest
+// folded angle between the central-difference vector e and the orientation's
+// three rotated cube axes (allen_cahn.py:28-39).  cos t = max_k |d_k.e|/|e|,
+// so with c2 = cos^2 t: cos^4 + sin^4 = c2^2 + (1 - c2)^2.  A zero (or
+// non-finite) |e| makes the reference's angles NaN, which it maps to 0, i.e.
+// c2 = 1; rounding above 1 is clamped the same way.
+__device__ __forceinline__ float aniso_factor(float A, float ex, float ey, float ez,
+                                              const float* d /* 9: 3 axes x (x,y,z) */) {
+  const float ee = ex * ex + ey * ey + ez * ez;
+  const float p0 = d[0] * ex + d[1] * ey + d[2] * ez;
+  const float p1 = d[3] * ex + d[4] * ey + d[5] * ez;
+  const float p2 = d[6] * ex + d[7] * ey + d[8] * ez;
+  const float m = fmaxf(fmaxf(p0 * p0, p1 * p1), p2 * p2);
+  float c2 = (ee > 0.f) ? fminf(m / ee, 1.f) : 1.f;
+  const float s2 = 1.f - c2;
+  return 1.f + A * (c2 * c2 + s2 * s2);
+}
+
+// ---------------------------------------------------------------------------
+// Heat equation (jax_am/cfd/gamma.py) per interior cell.
+// ---------------------------------------------------------------------------
+struct HeatConsts {
+  int nx, ny, nz;
+  float dx, dy, dz;
+  float dx2, dy2, dz2;       // d^2
+  float rho, h, sb_eps, T0, T0_4, Ts, Tl, Tl_minus_Ts, latent;
+  float beam_coef;           // 2 * absorptivity / pi / r^2  (times P gives the peak flux)
+  float two_over_r2;         // 2 / r^2
+  float x_first, y_first;
+};
+
+__device__ __forceinline__ float heat_k(const HeatConsts& H, float T) {
+  return 0.0163f * fminf(fmaxf(T, 300.f), H.Tl) + 4.5847f;  // gamma.py:14
+}
+
+// Robin + radiation flux magnitude h (Tf - T0) + SB eps (Tf^4 - T0^4)
+// evaluated at the face temperature Tf (gamma.py:23-34).
+__device__ __forceinline__ float heat_robin(const HeatConsts& H, float Tf) {
+  const float t2 = Tf * Tf;
+  return H.h * (Tf - H.T0) + H.sb_eps * (t2 * t2 - H.T0_4);
+}
+
+// Evaluate the beam position and power at time t from the tool path.
+__device__ __forceinline__ void laser_at(const pfg_heat_params& hp, double t, float* xl,
+                                         float* yl, float* P) {
+  *xl = 0.f; *yl = 0.f; *P = 0.f;
+  for (int s = 0; s < hp.num_segments && s < PFG_MAX_SEGMENTS; ++s) {
+    const pfg_segment& g = hp.path[s];
+    if (t >= (double)g.t0 && t < (double)g.t1) {
+      const double f = (t - (double)g.t0) / ((double)g.t1 - (double)g.t0);
+      *xl = (float)((double)g.x0 + f * ((double)g.x1 - (double)g.x0));
+      *yl = (float)((double)g.y0 + f * ((double)g.y1 - (double)g.y0));
+      *P = g.power;
+      return;
+    }
+  }
+}
+
+// One explicit heat update of interior cell (gx, gy, gz) given its old value
+// and its six old neighbours in the ghosted field (a neighbour across a
+// domain face is the old ghost).  idx is the cell's index in the ghosted
+// array and sx, sy, sz its element strides.  New ghosts of the faces this cell touches
+// are computed from the old ghost and written to Tg_out (gamma.py:18-43);
+// the Laplacian uses them (gamma.py:58-60).  Returns the new interior value.
+__device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc, float Txm,
+                                                  float Txp, float Tym, float Typ, float Tzm,
+                                                  float Tzp, int gx, int gy, int gz, float xl,
+                                                  float yl, float P, float dt, float* Tg_out,
+                                                  int64_t idx, int64_t sx, int64_t sy,
+                                                  int64_t sz) {
+  const float k = heat_k(H, Tc);
+  const float Tcl = fminf(fmaxf(Tc, H.Ts), H.Tl);
+  const float fl = (Tcl - H.Ts) / H.Tl_minus_Ts;
+  const float cp = 0.2441f * fminf(fmaxf(Tc, 300.f), H.Tl) + 338.39f +
+                   ((fl > 0.f && fl < 1.f) ? H.latent : 0.f);  // gamma.py:12-15
+  if (gx == 0) {
+    Txm = Tc - (heat_robin(H, (Tc + Txm) * 0.5f) / k) * H.dx;
+    Tg_out[idx - sx] = Txm;
+  }
+  if (gx == H.nx - 1) {
+    Txp = Tc - (heat_robin(H, (Tc + Txp) * 0.5f) / k) * H.dx;
+    Tg_out[idx + sx] = Txp;
+  }
+  if (gy == 0) {
+    Tym = Tc - (heat_robin(H, (Tc + Tym) * 0.5f) / k) * H.dy;
+    Tg_out[idx - sy] = Tym;
+  }
+  if (gy == H.ny - 1) {
+    Typ = Tc - (heat_robin(H, (Tc + Typ) * 0.5f) / k) * H.dy;
+    Tg_out[idx + sy] = Typ;
+  }
+  if (gz == 0) {
+    Tzm = Tc - (heat_robin(H, (Tc + Tzm) * 0.5f) / k) * H.dz;
+    Tg_out[idx - sz] = Tzm;
+  }
+  if (gz == H.nz - 1) {
+    // top face: convection + radiation minus the Gaussian beam flux (gamma.py:33-35)
+    const float x = H.x_first + (float)gx * H.dx;
+    const float y = H.y_first + (float)gy * H.dy;
+    const float ddx = x - xl, ddy = y - yl;
+    const float beam = P * H.beam_coef * expf(-(ddx * ddx + ddy * ddy) * H.two_over_r2);
+    const float q = heat_robin(H, (Tc + Tzp) * 0.5f) - beam;
+    Tzp = Tc - (q / k) * H.dz;
+    Tg_out[idx + sz] = Tzp;
+  }
+  const float txx = (Txm - 2.f * Tc + Txp) / H.dx2;  // gamma.py:49-51
+  const float tyy = (Tym - 2.f * Tc + Typ) / H.dy2;
+  const float tzz = (Tzm - 2.f * Tc + Tzp) / H.dz2;
+  return Tc + dt * ((k / H.rho / cp) * (txx + tyy + tzz));
+}
+
+HeatConsts make_heat_consts(const pfg_heat_params& h);
+PFConsts make_pf_consts(const pfg_pf_params& p);
+
+}  // namespace pfg

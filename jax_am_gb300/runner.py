@@ -1,0 +1,177 @@
+"""Resident, graph-replayed time stepping on one GPU.
+
+The reference drives every step from a Python loop with one host-to-device
+dispatch per step (``applications/phase_field/solidification/example.py:83``,
+``applications/cfd/gamma/example.py:111-113``).  Here the state stays in HBM
+in double buffers, the simulation clock lives on the device (each step reads
+one clock and writes the other), and a CUDA graph of an even number of steps
+is captured once and replayed, so a run of K steps costs K kernel launches
+from one graph launch per replay and no host round trip.
+
+* ``QuenchRun``: phase field under the moving linear gradient of the
+  directional-solidification driver, T evaluated inside the kernel.
+* ``HeatPFRun``: the fused heat + phase-field step with a tool-path laser.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .cfd.gamma import make_heat_params, stable_dt as heat_stable_dt
+from .phase_field.allen_cahn import PFSolver, Quench
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class _GraphRun:
+    graph_steps = 20  # steps per captured graph (even: buffers return to their start)
+
+    def __init__(self):
+        self.cur = 0
+        self.clk = torch.zeros((2, 2), dtype=torch.int64, device="cuda")
+        self._graph = None
+        self.launches = 0
+
+    def _launch(self, src):
+        raise NotImplementedError
+
+    def step(self):
+        """One eager step."""
+        self._launch(self.cur)
+        self.cur ^= 1
+
+    def _capture(self):
+        # one eager step first: kernel attributes are configured outside the capture
+        self.step()
+        g = torch.cuda.CUDAGraph()
+        start, counted = self.cur, self.launches
+        with torch.cuda.graph(g):
+            src = start
+            for _ in range(self.graph_steps):
+                self._launch(src)
+                src ^= 1
+        self.launches = counted  # captured launches run at replay, counted there
+        self._graph = g
+        return 1
+
+    def run(self, steps, graph=True):
+        """Advance ``steps`` steps (graph replay when ``graph``)."""
+        done = 0
+        if graph and steps >= self.graph_steps:
+            if self._graph is None:
+                done += self._capture()
+            while steps - done >= self.graph_steps:
+                self._graph.replay()
+                self.launches += self.graph_steps
+                done += self.graph_steps
+        while done < steps:
+            self.step()
+            done += 1
+        return self
+
+    def set_time(self, t, step=0):
+        c = self.clk[self.cur]
+        c[1] = int(step)
+        c[0:1].view(torch.float64)[0] = float(t)
+
+    @property
+    def t(self):
+        return float(self.clk[self.cur][0:1].view(torch.float64).item())
+
+    @property
+    def steps_taken(self):
+        return int(self.clk[self.cur][1].item())
+
+
+class QuenchRun(_GraphRun):
+    """Phase field under a ``Quench`` gradient, state resident on the GPU."""
+
+    def __init__(self, solver: PFSolver, quench: Quench, dt, eta0=None, t0=0.0):
+        super().__init__()
+        self.solver = solver
+        self.quench = quench
+        self.q = quench.struct(solver.params.h_z)
+        self.dt = float(dt)
+        e0 = solver.ini_cond() if eta0 is None else eta0
+        self.eta = [e0.contiguous().clone(), torch.empty_like(e0)]
+        self.set_time(t0)
+
+    def _launch(self, src):
+        s = self.solver
+        st = s.lib.pfg_pf_step_quench(ctypes.byref(s.params), ctypes.byref(self.q),
+                                       _lib.ptr(self.eta[src]), _lib.ptr(self.eta[src ^ 1]),
+                                       _lib.ptr(self.clk[src]), _lib.ptr(self.clk[src ^ 1]),
+                                       self.dt, _stream())
+        _lib.check(st, "pfg_pf_step_quench")
+        self.launches += 1
+
+    @property
+    def state(self):
+        return self.eta[self.cur]
+
+
+def single_track(x_start, y, speed, power, t_end, t_start=0.0):
+    """Tool path of one straight track along +x."""
+    return [(t_start, t_end, x_start, y, x_start + speed * (t_end - t_start), y, power)]
+
+
+def raster(tracks, speed, power, x_start, x_end, t_start=0.0):
+    """Sequential tracks along +x at the given y positions, one after the
+    other, as the reference's multi-track raster (``applications/phase_field/
+    multi_scan/pf_params.yaml:84-88``) scans them."""
+    segs, t = [], t_start
+    for y in tracks:
+        dur = (x_end - x_start) / speed
+        segs.append((t, t + dur, x_start, y, x_end, y, power))
+        t += dur
+    return segs
+
+
+class HeatPFRun(_GraphRun):
+    """Fused explicit heat + phase-field run with a tool-path laser."""
+
+    def __init__(self, solver: PFSolver, gamma_args, path, dt=None, eta0=None, T_init=None,
+                 t0=0.0):
+        super().__init__()
+        self.solver = solver
+        p = solver.params
+        self.heat = make_heat_params(gamma_args, p.nx, p.ny, p.nz, p.h_x, p.h_y, p.h_z,
+                                     layout=_lib.LAYOUT_ZYX, path=path)
+        if dt is None:
+            dt = min(solver.stable_dt(), heat_stable_dt(gamma_args, p.h_x, p.h_y, p.h_z))
+        self.dt = float(dt)
+        e0 = solver.ini_cond() if eta0 is None else eta0
+        self.eta = [e0.contiguous().clone(), torch.empty_like(e0)]
+        shape = (p.nz + 2, p.ny + 2, p.nx + 2)
+        if T_init is None:
+            Tg = torch.full(shape, float(gamma_args["T0"]), dtype=torch.float32, device="cuda")
+        else:
+            Tg = T_init.to("cuda", torch.float32).reshape(shape).contiguous()
+        self.Tg = [Tg.clone(), Tg.clone()]  # edge ghosts stay equal in both buffers
+        self.set_time(t0)
+
+    def _launch(self, src):
+        s = self.solver
+        st = s.lib.pfg_heat_pf_step(ctypes.byref(s.params), ctypes.byref(self.heat),
+                                     _lib.ptr(self.eta[src]), _lib.ptr(self.eta[src ^ 1]),
+                                     _lib.ptr(self.Tg[src]), _lib.ptr(self.Tg[src ^ 1]),
+                                     _lib.ptr(self.clk[src]), _lib.ptr(self.clk[src ^ 1]),
+                                     self.dt, _stream())
+        _lib.check(st, "pfg_heat_pf_step")
+        self.launches += 1
+
+    @property
+    def state(self):
+        return self.eta[self.cur]
+
+    @property
+    def T_ghosted(self):
+        return self.Tg[self.cur]
+
+    @property
+    def T_cells(self):
+        """(N, 1) interior temperature in the phase-field cell order."""
+        return self.Tg[self.cur][1:-1, 1:-1, 1:-1].reshape(-1, 1)

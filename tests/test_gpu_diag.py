@@ -1,0 +1,53 @@
+"""The on-device diagnostics (PFSolver.inspect_sol's metrics, float64 energy
+and mass, argmax map) against the oracle."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import pf_oracle as O
+from tests.cases import f32, pf_case
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from jax_am_gb300 import _build
+    _build.build()
+
+
+@pytest.mark.parametrize("shape,n,bc", [((9, 7, 5), 5, None), ((17, 13, 6), 20, "periodic"),
+                                        ((4, 4, 4), 33, None), ((31, 2, 3), 64, None)])
+def test_diag_vs_oracle(shape, n, bc):
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    poly, eta, T, pf_args, oargs, obc = pf_case(shape, n, 0.0, seed=12, bc=bc)
+    s = PFSolver(pf_args, poly)
+    eta0 = np.roll(eta, 1, axis=1)
+    ties = np.zeros(n)
+    ties[[0, n - 1]] = 0.7  # a tie: first maximum wins
+    eta[0] = ties
+    eta[1] = 0.0  # all zero: index 0
+    d = s.diagnostics(eta, T, eta0)
+    m = O.inspect(eta, eta0, T, oargs["T_liquidus"])
+    assert d["n_ori_changed"] == round(m["pct_ori_changed"] * len(eta) / 100)
+    assert d["pct_liquid"] == pytest.approx(m["pct_liquid"], abs=1e-12)
+    assert d["max_T"] == m["max_T"]
+    assert d["n_nonfinite"] == 0
+    np.testing.assert_allclose(d["mass"], eta.sum(axis=0), rtol=1e-12)
+    e_ref = O.free_energy(eta, T, oargs, None, obc)
+    assert d["energy"] == pytest.approx(e_ref, rel=1e-9)
+    am = s.argmax(torch.tensor(eta, dtype=torch.float32, device="cuda")).cpu().numpy()
+    np.testing.assert_array_equal(am, np.argmax(eta.astype(np.float32), axis=1))
+
+
+def test_inspect_sol_raises_on_nan(capsys):
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    poly, eta, T, pf_args, oargs, obc = pf_case((5, 5, 5), 4, 0.0, seed=13)
+    s = PFSolver(pf_args, poly)
+    eta[17, 2] = np.nan
+    eta[33, 0] = np.inf
+    d = s.diagnostics(eta, T)
+    assert d["n_nonfinite"] == 2
+    with pytest.raises(ValueError):
+        s.inspect_sol(eta, eta, T, np.arange(11), 10)
+    assert "percent of change of orientations" in capsys.readouterr().out
