@@ -24,7 +24,7 @@ def test_diag_vs_oracle(shape, n, bc):
     s = PFSolver(pf_args, poly)
     eta0 = np.roll(eta, 1, axis=1)
     ties = np.zeros(n)
-    ties[[0, n - 1]] = 0.7  # a tie: first maximum wins
+    ties[[0, n - 1]] = np.float32(0.7)  # a tie: first maximum wins
     eta[0] = ties
     eta[1] = 0.0  # all zero: index 0
     d = s.diagnostics(eta, T, eta0)
