@@ -148,6 +148,12 @@ const char* pfg_last_cuda_error(void);
  * 5 pfg_quench. */
 int64_t pfg_struct_size(int which);
 
+/* Kernel selection for the stencil steps: 0 (default) uses the warp-per-cells
+ * kernel whenever num_oris / VEC <= 32 (VEC = 4, 2 or 1: the largest width
+ * dividing num_oris) and the generic kernel otherwise; 1 always uses the
+ * generic kernel.  Both compute the same update.  Process-wide setting. */
+int pfg_set_kernel_variant(int variant);
+
 /* ---- phase field --------------------------------------------------------
  * One explicit Euler step of the Allen-Cahn grain-growth model with the
  * temperature held at T (the start-of-step value):

@@ -76,6 +76,7 @@ _PROTOS = {
     "pfg_status_string": (ctypes.c_char_p, [_I]),
     "pfg_last_cuda_error": (ctypes.c_char_p, []),
     "pfg_struct_size": (ctypes.c_int64, [_I]),
+    "pfg_set_kernel_variant": (_I, [_I]),
     "pfg_pf_step": (_I, [ctypes.POINTER(PfParams), _P, _P, _P, _F, _P]),
     "pfg_pf_step_quench": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(Quench), _P, _P, _P, _P,
                                 _F, _P]),

@@ -22,33 +22,9 @@
 
 #include "pfg_device.cuh"
 #include "pfg_host.h"
+#include "pfg_step.cuh"
 
 namespace pfg {
-
-// Where the phase field takes its temperature from.
-enum TSource { kTArray = 0, kTHeat = 1, kTQuench = 2 };
-
-struct StepArgs {
-  int nx, ny, nz, n;
-  int bcx, bcy, bcz;
-  float dt;
-  PFConsts pc;
-  // tiling
-  int tx, ty, zc, stages, pitch, tslot, tpc, rs;
-  int tiles_x, tiles_y, zchunks;
-  // buffers
-  const float* eta_in;
-  float* eta_out;
-  const float* T;  // per-cell T (pf only) or ghosted Tg (fused)
-  float* T_out;    // ghosted Tg_out (fused) or nullptr
-  const pfg_clock* clk_in;
-  pfg_clock* clk_out;
-  HeatConsts hc;
-  pfg_heat_params hp;  // tool path (fused)
-  pfg_quench q;        // moving gradient (quench)
-  float h_z;
-  float dirs[3 * PFG_MAX_ORIS * 3];
-};
 
 template <int VEC>
 __device__ __forceinline__ void stage_copy(float* dst, const float* src) {
@@ -421,14 +397,39 @@ int check_heat_params(const pfg_heat_params* h) {
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
+int g_kernel_variant = 0;
+
 TilePlan plan_for_current_device(const pfg_pf_params& p) {
   const DeviceInfo& d = device_info();
   return plan_tiles(p.nx, p.ny, p.nz, p.num_oris, d.sm_count, d.smem_per_sm, d.smem_per_block);
 }
 
+// Plan and launch one step: the warp-per-cells kernel when the orientation
+// count allows it (num_oris / VEC <= 32), otherwise the generic kernel.
+template <int TSRC>
+static cudaError_t dispatch(StepArgs& a, const pfg_pf_params& p, float dt, cudaStream_t s) {
+  const DeviceInfo& d = device_info();
+  TilePlan t;
+  if (g_kernel_variant == 0 &&
+      plan_warp_tiles(p.nx, p.ny, p.nz, p.num_oris, d.sm_count, d.smem_per_sm, &t)) {
+    fill_common(a, p, t, dt);
+    a.cpw = t.cpw; a.wx = t.wx; a.rpw = t.rpw;
+    return launch_warp_kernel<TSRC>(a, t, s);
+  }
+  t = plan_for_current_device(p);
+  fill_common(a, p, t, dt);
+  return launch_a<TSRC>(a, t, s);
+}
+
 }  // namespace pfg
 
 using namespace pfg;
+
+extern "C" int pfg_set_kernel_variant(int variant) {
+  if (variant != 0 && variant != 1) return PFG_ERR_PARAM;
+  g_kernel_variant = variant;
+  return PFG_OK;
+}
 
 extern "C" int pfg_pf_step(const pfg_pf_params* p, const float* eta_in, float* eta_out,
                            const float* T, float dt, void* stream) {
@@ -437,13 +438,10 @@ extern "C" int pfg_pf_step(const pfg_pf_params* p, const float* eta_in, float* e
   if (!eta_in || !eta_out || !T) return PFG_ERR_NULL;
   if (!aligned16(eta_in) || !aligned16(eta_out)) return PFG_ERR_ALIGN;
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
-  const TilePlan t = plan_for_current_device(*p);
   StepArgs a{};
-  fill_common(a, *p, t, dt);
   a.eta_in = eta_in; a.eta_out = eta_out; a.T = T; a.T_out = nullptr;
   a.clk_in = nullptr; a.clk_out = nullptr;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return record_cuda(launch_a<kTArray>(a, t, s));
+  return record_cuda(dispatch<kTArray>(a, *p, dt, static_cast<cudaStream_t>(stream)));
 }
 
 extern "C" int pfg_pf_step_quench(const pfg_pf_params* p, const pfg_quench* q,
@@ -455,13 +453,11 @@ extern "C" int pfg_pf_step_quench(const pfg_pf_params* p, const pfg_quench* q,
   if (clk_in == clk_out) return PFG_ERR_PARAM;
   if (!aligned16(eta_in) || !aligned16(eta_out)) return PFG_ERR_ALIGN;
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
-  const TilePlan t = plan_for_current_device(*p);
   StepArgs a{};
-  fill_common(a, *p, t, dt);
   a.eta_in = eta_in; a.eta_out = eta_out; a.T = nullptr; a.T_out = nullptr;
   a.clk_in = clk_in; a.clk_out = clk_out;
   a.q = *q;
-  return record_cuda(launch_a<kTQuench>(a, t, static_cast<cudaStream_t>(stream)));
+  return record_cuda(dispatch<kTQuench>(a, *p, dt, static_cast<cudaStream_t>(stream)));
 }
 
 extern "C" int pfg_heat_pf_step(const pfg_pf_params* p, const pfg_heat_params* h,
@@ -479,13 +475,10 @@ extern "C" int pfg_heat_pf_step(const pfg_pf_params* p, const pfg_heat_params* h
   if (clk_in == clk_out) return PFG_ERR_PARAM;
   if (!aligned16(eta_in) || !aligned16(eta_out)) return PFG_ERR_ALIGN;
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
-  const TilePlan t = plan_for_current_device(*p);
   StepArgs a{};
-  fill_common(a, *p, t, dt);
   a.eta_in = eta_in; a.eta_out = eta_out; a.T = Tg_in; a.T_out = Tg_out;
   a.clk_in = clk_in; a.clk_out = clk_out;
   a.hc = make_heat_consts(*h);
   a.hp = *h;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  return record_cuda(launch_a<kTHeat>(a, t, s));
+  return record_cuda(dispatch<kTHeat>(a, *p, dt, static_cast<cudaStream_t>(stream)));
 }

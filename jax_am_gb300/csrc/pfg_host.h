@@ -26,6 +26,7 @@ int record_cuda(cudaError_t e);
 
 // Tiling of the z-marching stencil kernel.
 struct TilePlan {
+  int cpw, wx, rpw;  // warp kernel: cells per warp, warps along x, rows per warp
   int vec;       // floats per thread chunk (4, 2 or 1: the largest dividing num_oris)
   int tpc;       // chunks per cell = num_oris / vec
   int tx, ty;    // tile cells along x and y
@@ -46,5 +47,7 @@ int check_pf_params(const pfg_pf_params* p);
 int check_heat_params(const pfg_heat_params* h);
 bool aligned16(const void* p);
 int vec_width(int n);
+// 0: pick the warp kernel when it applies; 1: always the generic kernel.
+extern int g_kernel_variant;
 
 }  // namespace pfg

@@ -1,0 +1,43 @@
+// Arguments of the stencil step kernels (internal).
+#pragma once
+
+#include "pfg_device.cuh"
+
+namespace pfg {
+
+// Where the phase field takes its temperature from.
+enum TSource { kTArray = 0, kTHeat = 1, kTQuench = 2 };
+
+struct StepArgs {
+  int nx, ny, nz, n;
+  int bcx, bcy, bcz;
+  float dt;
+  PFConsts pc;
+  // tiling (generic kernel: rs rows in flight; warp-cell kernel: wx x wy warps,
+  // cpw cells per warp, rpw rows per warp)
+  int tx, ty, zc, stages, pitch, tslot, tpc, rs;
+  int tiles_x, tiles_y, zchunks;
+  int cpw, wx, rpw;
+  // buffers
+  const float* eta_in;
+  float* eta_out;
+  const float* T;  // per-cell T (pf only) or ghosted Tg (fused)
+  float* T_out;    // ghosted Tg_out (fused) or nullptr
+  const pfg_clock* clk_in;
+  pfg_clock* clk_out;
+  HeatConsts hc;
+  pfg_heat_params hp;  // tool path (fused)
+  pfg_quench q;        // moving gradient (quench)
+  float h_z;
+  float dirs[3 * PFG_MAX_ORIS * 3];
+};
+
+
+struct TilePlan;
+// Warp-per-cells kernel (pf_fast.cu).
+bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
+                     TilePlan* out);
+template <int TSRC>
+cudaError_t launch_warp_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);
+
+}  // namespace pfg

@@ -105,10 +105,20 @@ def _laser_fn(path):
     return laser
 
 
+@pytest.fixture(params=[0, 1], ids=["warp", "generic"])
+def variant(request):
+    from jax_am_gb300 import _lib
+    lib = _lib.load()
+    assert lib.pfg_set_kernel_variant(request.param) == 0
+    yield request.param
+    lib.pfg_set_kernel_variant(0)
+
+
 @pytest.mark.parametrize("shape,n,aniso,steps", [((12, 10, 8), 5, 0.15, 6),
                                                  ((33, 17, 9), 20, 0.15, 4),
-                                                 ((7, 9, 5), 10, 0.0, 5)])
-def test_fused_heat_pf_vs_oracle(shape, n, aniso, steps):
+                                                 ((7, 9, 5), 10, 0.0, 5),
+                                                 ((50, 26, 12), 30, 0.15, 3)])
+def test_fused_heat_pf_vs_oracle(shape, n, aniso, steps, variant):
     from jax_am_gb300.phase_field.allen_cahn import PFSolver
     from jax_am_gb300.runner import HeatPFRun, single_track
     poly, eta, _, pf_args, oargs, obc = pf_case(shape, n, aniso, seed=21, h=(1e-6, 1e-6, 1e-6))

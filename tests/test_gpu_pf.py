@@ -25,6 +25,16 @@ def _built():
     _build.build()
 
 
+@pytest.fixture(params=[0, 1], ids=["warp", "generic"])
+def variant(request):
+    """Run a test on the warp-per-cells kernel and on the generic kernel."""
+    from jax_am_gb300 import _lib
+    lib = _lib.load()
+    assert lib.pfg_set_kernel_variant(request.param) == 0
+    yield request.param
+    lib.pfg_set_kernel_variant(0)
+
+
 def _solver(pf_args, poly):
     from jax_am_gb300.phase_field.allen_cahn import PFSolver
     return PFSolver(pf_args, poly)
@@ -56,7 +66,7 @@ def _argmax_mismatch(a, b):
 
 
 @pytest.mark.parametrize("name", ["pf_iso.npz", "pf_aniso.npz", "pf_aniso_n20.npz"])
-def test_matches_reference_golden(name):
+def test_matches_reference_golden(name, variant):
     d = np.load(os.path.join(G, name))
     keys = ("dim", "T_liquidus", "gas_const", "Qg", "L0", "kappa_g", "m_g", "ad_hoc")
 
@@ -96,7 +106,7 @@ CASES = [
 
 
 @pytest.mark.parametrize("shape,n,aniso,bc,force", CASES)
-def test_random_vs_oracle(shape, n, aniso, bc, force):
+def test_random_vs_oracle(shape, n, aniso, bc, force, variant):
     poly, eta, T, pf_args, oargs, obc = pf_case(shape, n, aniso, seed=hash((shape, n)) & 0xffff,
                                                 bc=bc, force=force)
     s = _solver(pf_args, poly)
@@ -106,12 +116,13 @@ def test_random_vs_oracle(shape, n, aniso, bc, force):
     ref = _run_oracle(eta, T, oargs, poly.unique_grain_directions, obc, dt, steps, force)
     err = np.abs(got - ref).max()
     mism = _argmax_mismatch(got, ref)
-    print(f"{shape} n={n} A={aniso} bc={bc}: max |d eta| = {err:.3e}, argmax mismatches = {mism}")
+    print(f"[{variant}] {shape} n={n} A={aniso} bc={bc}: max |d eta| = {err:.3e}, "
+          f"argmax mismatches = {mism}")
     assert err <= ETA_TOL
     assert mism == 0
 
 
-def test_many_steps_directional_solidification():
+def test_many_steps_directional_solidification(variant):
     """Config-1 physics on a reduced grid: Voronoi polycrystal, moving
     gradient 1e6 K/m at 0.1 m/s with the front mid-height, liquid forcing,
     200 steps at the stable dt; state compared after every 50 steps."""
@@ -174,7 +185,7 @@ def test_ini_cond_one_hot():
                                   O.ini_cond(poly.cell_ori_inds, 9))
 
 
-def test_uniform_grain_is_stationary():
+def test_uniform_grain_is_stationary(variant):
     """One-hot eta in a uniform solid grain: rhs = m_g (1 - 1) = 0 and a zero
     Laplacian, so the step leaves it unchanged exactly."""
     poly, eta, T, pf_args, oargs, obc = pf_case((8, 8, 8), 6, 0.15, seed=5, noise=0.0)
@@ -201,3 +212,19 @@ def test_liquid_decay_rate():
     expect = e - dt * Lg * 2.4e5 * (e ** 3 - e + 4 * e * (S - e ** 2) + 2 * e)
     np.testing.assert_allclose(got[0], expect, atol=1e-6)
     np.testing.assert_allclose(got, np.tile(got[0], (64, 1)), atol=0)
+
+
+@pytest.mark.parametrize("n,aniso", [(20, 0.15), (10, 0.15), (30, 0.0), (7, 0.15)])
+def test_warp_and_generic_kernels_agree(n, aniso):
+    """Both kernels compute the same update; they differ only in float32
+    rounding (packed FMAs, approximate reciprocal in the anisotropy)."""
+    from jax_am_gb300 import _lib
+    lib = _lib.load()
+    poly, eta, T, pf_args, oargs, obc = pf_case((41, 29, 13), n, aniso, seed=n)
+    outs = []
+    for v in (0, 1):
+        lib.pfg_set_kernel_variant(v)
+        s = _solver(pf_args, poly)
+        outs.append(_run_gpu(s, eta, T, 1e-8, 4))
+    lib.pfg_set_kernel_variant(0)
+    assert np.abs(outs[0] - outs[1]).max() <= 1e-5
