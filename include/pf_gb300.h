@@ -154,6 +154,18 @@ int64_t pfg_struct_size(int which);
  * generic kernel.  Both compute the same update.  Process-wide setting. */
 int pfg_set_kernel_variant(int variant);
 
+/* Tile-plan overrides of the warp-per-cells kernel for tuning sweeps
+ * (value 0 restores the automatic choice): key 0 = warps along x (1, 2, 4, 8),
+ * 1 = rows per warp (1..32), 2 = shared-memory plane slots (4..6),
+ * 3 = z chunks per tile column.  Process-wide; results do not change. */
+int pfg_tune(int key, int value);
+
+/* The launch plan a step with these parameters would use on the current
+ * device, as 12 int32: kernel (0 warp-per-cells, 1 generic), VEC, lanes per
+ * cell, tile x, tile y, warps along x, rows per warp, plane slots, planes per
+ * unit, CTAs, dynamic shared memory bytes, SM count. */
+int pfg_describe_plan(const pfg_pf_params* p, int32_t* out);
+
 /* ---- phase field --------------------------------------------------------
  * One explicit Euler step of the Allen-Cahn grain-growth model with the
  * temperature held at T (the start-of-step value):

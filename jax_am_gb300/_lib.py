@@ -77,6 +77,8 @@ _PROTOS = {
     "pfg_last_cuda_error": (ctypes.c_char_p, []),
     "pfg_struct_size": (ctypes.c_int64, [_I]),
     "pfg_set_kernel_variant": (_I, [_I]),
+    "pfg_tune": (_I, [_I, _I]),
+    "pfg_describe_plan": (_I, [ctypes.POINTER(PfParams), _P]),
     "pfg_pf_step": (_I, [ctypes.POINTER(PfParams), _P, _P, _P, _F, _P]),
     "pfg_pf_step_quench": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(Quench), _P, _P, _P, _P,
                                 _F, _P]),
@@ -137,3 +139,14 @@ def check(status, what):
 def ptr(t):
     """Device address of a tensor (None -> NULL)."""
     return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+PLAN_FIELDS = ("kernel", "vec", "lanes_per_cell", "tile_x", "tile_y", "warps_x", "rows_per_warp",
+               "slots", "planes_per_unit", "ctas", "smem_bytes", "sm_count")
+
+
+def describe_plan(params):
+    """The launch plan of a step with ``params`` on the current device."""
+    out = (ctypes.c_int32 * 12)()
+    check(load().pfg_describe_plan(ctypes.byref(params), out), "pfg_describe_plan")
+    return dict(zip(PLAN_FIELDS, list(out)))

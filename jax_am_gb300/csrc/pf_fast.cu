@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include "pfg_host.h"
 #include "pfg_step.cuh"
@@ -184,7 +185,6 @@ __global__ void __launch_bounds__(kThreads, 2) pf_warp_kernel(const __grid_const
   const int xs = wxi * a.cpw + (lane_active ? lc : 0);
   const bool col_valid = lane_active && xs < txv;
   const int i0 = k * VEC;
-  const int seg_base = (lane_active ? lc : 0) * tpc;
 
   constexpr int NP = (VEC >= 2) ? VEC / 2 : 1;  // orientation pairs per lane
   float2 dpair[ANISO && VEC >= 2 ? 9 * NP : 1];
@@ -235,14 +235,44 @@ __global__ void __launch_bounds__(kThreads, 2) pf_warp_kernel(const __grid_const
                              dst_cell0, magic_rc, magic_tx2, magic_txv);
   };
 
-  // per-cell temperature coefficients of plane pz (staged in slot) -> cc[buf]
-  auto cell_coefs = [&](int slot, int buf) {
+  // per-cell coefficients of the plane staged in `slot` -> cc[buf]:
+  // (cg, cl, K = 4 S + 2 (1 - zeta)^2 - 1, liquid) with S = sum_i eta_i^2
+  auto cell_coefs = [&](int slot, int buf, int pz) {
+    const float* es = eta_s + (size_t)slot * slot_floats;
     const float* ts = T_s + (size_t)slot * a.tslot;
     float4* cb = cc + (size_t)buf * a.ty * a.tx;
+    TempCoef plane{};
+    if constexpr (TSRC == kTQuench) {
+      const double zc = a.q.z_first + (double)pz * (double)a.h_z;
+      const float Tz = (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t0);
+      plane = temp_coefficients(a.pc, Tz, a.dt);
+    }
     for (int i = threadIdx.x; i < tyv * txv; i += kThreads) {
       const int r = fast_div(i, magic_txv), c = i - r * txv;
-      const TempCoef tc = temp_coefficients(a.pc, ts[(r + 1) * (a.tx + 2) + c + 1], a.dt);
-      cb[r * a.tx + c] = make_float4(tc.cg, tc.cl, tc.om2, tc.liquid);
+      const float* ce = es + (r + 1) * a.pitch + (c + 1) * n;
+      float s0 = 0.f, s1 = 0.f;
+      int q = 0;
+      for (; q + 2 * VEC <= n; q += 2 * VEC) {
+        VecF<VEC> u, v;
+        u.load(ce + q);
+        v.load(ce + q + VEC);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+          s0 = fmaf(u.v[e], u.v[e], s0);
+          s1 = fmaf(v.v[e], v.v[e], s1);
+        }
+      }
+      for (; q < n; q += VEC) {
+        VecF<VEC> u;
+        u.load(ce + q);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) s0 = fmaf(u.v[e], u.v[e], s0);
+      }
+      const float S_ = s0 + s1;
+      TempCoef tc;
+      if constexpr (TSRC == kTQuench) tc = plane;
+      else tc = temp_coefficients(a.pc, ts[(r + 1) * (a.tx + 2) + c + 1], a.dt);
+      cb[r * a.tx + c] = make_float4(tc.cg, tc.cl, 4.f * S_ + tc.om2 - 1.f, tc.liquid);
     }
   };
 
@@ -252,11 +282,9 @@ __global__ void __launch_bounds__(kThreads, 2) pf_warp_kernel(const __grid_const
     if (pz <= ze) stage(p % S, pz);
     cp_async_commit();
   }
-  if constexpr (TSRC != kTQuench) {
-    cp_async_wait(S - 4);
-    __syncthreads();
-    cell_coefs(1, 0);  // plane zb sits in slot 1
-  }
+  cp_async_wait(S - 4);
+  __syncthreads();
+  cell_coefs(1, 0, zb);  // plane zb sits in slot 1
 
   const int64_t plane_elems = (int64_t)a.ny * a.nx * n;
   for (int z = zb; z < ze; ++z) {
@@ -288,45 +316,18 @@ __global__ void __launch_bounds__(kThreads, 2) pf_warp_kernel(const __grid_const
         a.T_out[idx] = Tn;
       }
     }
-    if constexpr (TSRC != kTQuench) {
-      if (z + 1 < ze) cell_coefs(s_next, (m + 1) & 1);
-    }
-    float4 plane_tc = make_float4(0.f, 0.f, 0.f, 0.f);
-    if constexpr (TSRC == kTQuench) {
-      const double zc = a.q.z_first + (double)z * (double)a.h_z;
-      const float Tz = (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t0);
-      const TempCoef tc = temp_coefficients(a.pc, Tz, a.dt);
-      plane_tc = make_float4(tc.cg, tc.cl, tc.om2, tc.liquid);
-    }
+    if (z + 1 < ze) cell_coefs(s_next, (m + 1) & 1, z + 1);
 
     // ---- element pass
     const float* e_cur = eta_s + (size_t)s_cur * slot_floats;
     const float* e_prev = eta_s + (size_t)s_prev * slot_floats;
     const float* e_next = eta_s + (size_t)s_next * slot_floats;
     const float4* ccb = cc + (size_t)(m & 1) * a.ty * a.tx;
-    for (int j = 0; j < a.rpw; ++j) {
-      const int r = wyi * a.rpw + j;
-      if (r >= tyv) break;  // warp-uniform
-      const int off = (r + 1) * a.pitch + (xs + 1) * n + i0;
-      VecF<VEC> c, xm, xp, ym, yp, zm, zp;
-      c.load(e_cur + off);
-      xm.load(e_cur + off - n);
-      xp.load(e_cur + off + n);
-      ym.load(e_cur + off - a.pitch);
-      yp.load(e_cur + off + a.pitch);
-      zm.load(e_prev + off);
-      zp.load(e_next + off);
-      float s = 0.f;
-#pragma unroll
-      for (int v = 0; v < VEC; ++v) s = fmaf(c.v[v], c.v[v], s);
-      // segmented sum over the cell's tpc lanes, then broadcast from its head
-      for (int o = 1; o < tpc; o <<= 1) {
-        const float t = __shfl_down_sync(0xffffffffu, s, o);
-        if (k + o < tpc) s += t;
-      }
-      const float Ssum = __shfl_sync(0xffffffffu, s, seg_base);
-      const float4 tc = (TSRC == kTQuench) ? plane_tc : ccb[r * a.tx + xs];
-      const float K = 4.f * Ssum + tc.z - 1.f;
+    const bool force = a.pc.force != 0;
+    auto row_update = [&](int r, const VecF<VEC>& c, const VecF<VEC>& xm, const VecF<VEC>& xp,
+                          const VecF<VEC>& ym, const VecF<VEC>& yp, const VecF<VEC>& zm,
+                          const VecF<VEC>& zp) {
+      const float4 tc = ccb[r * a.tx + xs];
       VecF<VEC> out;
       if constexpr (VEC >= 2) {
 #pragma unroll
@@ -336,15 +337,15 @@ __global__ void __launch_bounds__(kThreads, 2) pf_warp_kernel(const __grid_const
               make_float2(xm.v[2 * p], xm.v[2 * p + 1]), make_float2(xp.v[2 * p], xp.v[2 * p + 1]),
               make_float2(ym.v[2 * p], ym.v[2 * p + 1]), make_float2(yp.v[2 * p], yp.v[2 * p + 1]),
               make_float2(zm.v[2 * p], zm.v[2 * p + 1]), make_float2(zp.v[2 * p], zp.v[2 * p + 1]),
-              &dpair[ANISO ? p * 9 : 0], f2(K), f2(tc.x), f2(tc.y));
+              &dpair[ANISO ? p * 9 : 0], f2(tc.z), f2(tc.x), f2(tc.y));
           out.v[2 * p] = o2.x;
           out.v[2 * p + 1] = o2.y;
         }
       } else {
         out.v[0] = update_one<ANISO>(a.pc, c.v[0], xm.v[0], xp.v[0], ym.v[0], yp.v[0], zm.v[0],
-                                     zp.v[0], dsc, K, tc.x, tc.y);
+                                     zp.v[0], dsc, tc.z, tc.x, tc.y);
       }
-      if (a.pc.force && tc.w != 0.f) {
+      if (force && tc.w != 0.f) {
 #pragma unroll
         for (int v = 0; v < VEC; ++v) out.v[v] = 0.f;
       }
@@ -353,6 +354,41 @@ __global__ void __launch_bounds__(kThreads, 2) pf_warp_kernel(const __grid_const
                           ((int64_t)(y0 + r) * a.nx + (x0 + xs)) * n + i0;
         out.store(a.eta_out + g);
       }
+    };
+    const int r_begin = wyi * a.rpw;
+    const int r_end = min(r_begin + a.rpw, tyv);
+    int r = r_begin;
+    for (; r + 1 < r_end; r += 2) {
+      // two rows share their y neighbours: rows r-1 .. r+2 are loaded once
+      const int off = (r + 1) * a.pitch + (xs + 1) * n + i0;
+      const int off2 = off + a.pitch;
+      VecF<VEC> ym, c, c2, yp2, xm, xp, xm2, xp2, zm, zp, zm2, zp2;
+      ym.load(e_cur + off - a.pitch);
+      c.load(e_cur + off);
+      c2.load(e_cur + off2);
+      yp2.load(e_cur + off2 + a.pitch);
+      xm.load(e_cur + off - n);
+      xp.load(e_cur + off + n);
+      xm2.load(e_cur + off2 - n);
+      xp2.load(e_cur + off2 + n);
+      zm.load(e_prev + off);
+      zp.load(e_next + off);
+      zm2.load(e_prev + off2);
+      zp2.load(e_next + off2);
+      row_update(r, c, xm, xp, ym, c2, zm, zp);
+      row_update(r + 1, c2, xm2, xp2, c, yp2, zm2, zp2);
+    }
+    if (r < r_end) {
+      const int off = (r + 1) * a.pitch + (xs + 1) * n + i0;
+      VecF<VEC> c, xm, xp, ym, yp, zm, zp;
+      c.load(e_cur + off);
+      xm.load(e_cur + off - n);
+      xp.load(e_cur + off + n);
+      ym.load(e_cur + off - a.pitch);
+      yp.load(e_cur + off + a.pitch);
+      zm.load(e_prev + off);
+      zp.load(e_next + off);
+      row_update(r, c, xm, xp, ym, yp, zm, zp);
     }
   }
   cp_async_wait(0);
@@ -362,6 +398,23 @@ __global__ void __launch_bounds__(kThreads, 2) pf_warp_kernel(const __grid_const
 // host side
 // ---------------------------------------------------------------------------
 
+// Plan overrides for tuning sweeps (0 = automatic).
+static int g_tune_wx = 0, g_tune_rpw = 0, g_tune_stages = 0, g_tune_zchunks = 0;
+
+int set_tune(int key, int value) {
+  if (value < 0) return PFG_ERR_PARAM;
+  switch (key) {
+    case 0: if (value && value != 1 && value != 2 && value != 4 && value != 8) return PFG_ERR_PARAM;
+            g_tune_wx = value; return PFG_OK;
+    case 1: if (value > 32) return PFG_ERR_PARAM;
+            g_tune_rpw = value; return PFG_OK;
+    case 2: if (value && (value < 4 || value > 6)) return PFG_ERR_PARAM;
+            g_tune_stages = value; return PFG_OK;
+    case 3: g_tune_zchunks = value; return PFG_OK;
+    default: return PFG_ERR_PARAM;
+  }
+}
+
 bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
                      TilePlan* out) {
   TilePlan t{};
@@ -369,16 +422,19 @@ bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
   t.tpc = n / t.vec;
   if (t.tpc > 32) return false;
   t.cpw = 32 / t.tpc;
-  t.stages = 4;
+  t.stages = g_tune_stages ? g_tune_stages : 4;
   const size_t budget = (size_t)max_smem_per_sm / 2 - 2048;  // two CTAs per SM
+  const long concurrent = 2L * sm_count;
   double best = 1e30;
   for (int wx = 1; wx <= 8; wx *= 2) {
+    if (g_tune_wx && wx != g_tune_wx) continue;
     const int wy = 8 / wx;
     const int tx = wx * t.cpw;
-    if (wx > 1 && (wx / 2) * t.cpw >= nx) continue;  // a narrower tile already covers x
+    if (!g_tune_wx && wx > 1 && (wx / 2) * t.cpw >= nx) continue;  // a narrower tile covers x
     for (int rpw = 1; rpw <= 32; ++rpw) {
+      if (g_tune_rpw && rpw != g_tune_rpw) continue;
       const int ty = wy * rpw;
-      if (rpw > 1 && wy * (rpw - 1) >= ny) break;
+      if (!g_tune_rpw && rpw > 1 && wy * (rpw - 1) >= ny) break;
       const int pitch = ((tx + 2) * n + 3) / 4 * 4;
       const int tslot = ((ty + 2) * (tx + 2) + 3) / 4 * 4;
       const size_t smem = (size_t)t.stages * ((size_t)(ty + 2) * pitch + tslot) * 4 +
@@ -387,7 +443,13 @@ bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
       const long tiles = (long)((nx + tx - 1) / tx) * ((ny + ty - 1) / ty);
       const double cover = (double)tiles * tx * ty / ((double)nx * ny);
       const double halo = (double)(tx + 2) * (ty + 2) / ((double)tx * ty);
-      const double score = cover * (0.75 + 0.25 * halo);
+      // wave quantisation of the units this tile gives
+      long zch = (4 * concurrent + tiles - 1) / tiles;
+      zch = std::max(1L, std::min(zch, (long)std::max(1, nz / 8)));
+      const long zc = (nz + zch - 1) / zch;
+      const double waves = (double)(tiles * ((nz + zc - 1) / zc)) / (double)concurrent;
+      const double wave_eff = waves / std::ceil(waves);
+      const double score = cover * (0.75 + 0.25 * halo) / wave_eff;
       if (score < best - 1e-9) {
         best = score;
         t.tx = tx; t.ty = ty; t.wx = wx; t.rpw = rpw;
@@ -399,10 +461,10 @@ bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
   t.rs = 0;
   t.tiles_x = (nx + t.tx - 1) / t.tx;
   t.tiles_y = (ny + t.ty - 1) / t.ty;
-  const long concurrent = 2L * sm_count;
   const long tiles = (long)t.tiles_x * t.tiles_y;
   long zch = (4 * concurrent + tiles - 1) / tiles;
   zch = std::max(1L, std::min(zch, (long)std::max(1, nz / 8)));
+  if (g_tune_zchunks) zch = std::min<long>(g_tune_zchunks, nz);
   t.zc = (int)((nz + zch - 1) / zch);
   t.zchunks = (nz + t.zc - 1) / t.zc;
   t.units = tiles * t.zchunks;

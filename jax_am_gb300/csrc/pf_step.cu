@@ -277,6 +277,9 @@ HeatConsts make_heat_consts(const pfg_heat_params& h) {
   c.nx = h.nx; c.ny = h.ny; c.nz = h.nz;
   c.dx = h.dx; c.dy = h.dy; c.dz = h.dz;
   c.dx2 = h.dx * h.dx; c.dy2 = h.dy * h.dy; c.dz2 = h.dz * h.dz;
+  c.rdx2 = 1.f / c.dx2; c.rdy2 = 1.f / c.dy2; c.rdz2 = 1.f / c.dz2;
+  c.inv_rho = 1.f / h.rho;
+  c.inv_dTsl = 1.f / (h.Tl - h.Ts);
   c.rho = h.rho;
   c.h = h.h_conv;
   c.sb_eps = (float)((double)h.sigma_sb * (double)h.emissivity);
@@ -424,6 +427,28 @@ static cudaError_t dispatch(StepArgs& a, const pfg_pf_params& p, float dt, cudaS
 }  // namespace pfg
 
 using namespace pfg;
+
+extern "C" int pfg_tune(int key, int value) { return set_tune(key, value); }
+
+extern "C" int pfg_describe_plan(const pfg_pf_params* p, int32_t* out) {
+  int st = check_pf_params(p);
+  if (st) return st;
+  if (!out) return PFG_ERR_NULL;
+  if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  const DeviceInfo& d = device_info();
+  TilePlan t;
+  int kernel = 0;
+  if (!(g_kernel_variant == 0 &&
+        plan_warp_tiles(p->nx, p->ny, p->nz, p->num_oris, d.sm_count, d.smem_per_sm, &t))) {
+    t = plan_for_current_device(*p);
+    kernel = 1;
+    t.wx = 0; t.rpw = 0;
+  }
+  const int32_t v[12] = {kernel, t.vec, t.tpc, t.tx, t.ty, t.wx, t.rpw, t.stages, t.zc,
+                         (int32_t)t.units, (int32_t)t.smem, d.sm_count};
+  for (int i = 0; i < 12; ++i) out[i] = v[i];
+  return PFG_OK;
+}
 
 extern "C" int pfg_set_kernel_variant(int variant) {
   if (variant != 0 && variant != 1) return PFG_ERR_PARAM;

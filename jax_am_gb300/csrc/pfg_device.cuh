@@ -158,6 +158,8 @@ struct HeatConsts {
   int nx, ny, nz;
   float dx, dy, dz;
   float dx2, dy2, dz2;       // d^2
+  float rdx2, rdy2, rdz2;    // 1/d^2
+  float inv_rho, inv_dTsl;   // 1/rho, 1/(Tl - Ts)
   float rho, h, sb_eps, T0, T0_4, Ts, Tl, Tl_minus_Ts, latent;
   float beam_coef;           // 2 * absorptivity / pi / r^2  (times P gives the peak flux)
   float two_over_r2;         // 2 / r^2
@@ -204,28 +206,29 @@ __device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc,
                                                   int64_t idx, int64_t sx, int64_t sy,
                                                   int64_t sz) {
   const float k = heat_k(H, Tc);
+  const float rk = __fdividef(1.f, k);
   const float Tcl = fminf(fmaxf(Tc, H.Ts), H.Tl);
-  const float fl = (Tcl - H.Ts) / H.Tl_minus_Ts;
+  const float fl = (Tcl - H.Ts) * H.inv_dTsl;
   const float cp = 0.2441f * fminf(fmaxf(Tc, 300.f), H.Tl) + 338.39f +
                    ((fl > 0.f && fl < 1.f) ? H.latent : 0.f);  // gamma.py:12-15
   if (gx == 0) {
-    Txm = Tc - (heat_robin(H, (Tc + Txm) * 0.5f) / k) * H.dx;
+    Txm = Tc - heat_robin(H, (Tc + Txm) * 0.5f) * rk * H.dx;
     Tg_out[idx - sx] = Txm;
   }
   if (gx == H.nx - 1) {
-    Txp = Tc - (heat_robin(H, (Tc + Txp) * 0.5f) / k) * H.dx;
+    Txp = Tc - heat_robin(H, (Tc + Txp) * 0.5f) * rk * H.dx;
     Tg_out[idx + sx] = Txp;
   }
   if (gy == 0) {
-    Tym = Tc - (heat_robin(H, (Tc + Tym) * 0.5f) / k) * H.dy;
+    Tym = Tc - heat_robin(H, (Tc + Tym) * 0.5f) * rk * H.dy;
     Tg_out[idx - sy] = Tym;
   }
   if (gy == H.ny - 1) {
-    Typ = Tc - (heat_robin(H, (Tc + Typ) * 0.5f) / k) * H.dy;
+    Typ = Tc - heat_robin(H, (Tc + Typ) * 0.5f) * rk * H.dy;
     Tg_out[idx + sy] = Typ;
   }
   if (gz == 0) {
-    Tzm = Tc - (heat_robin(H, (Tc + Tzm) * 0.5f) / k) * H.dz;
+    Tzm = Tc - heat_robin(H, (Tc + Tzm) * 0.5f) * rk * H.dz;
     Tg_out[idx - sz] = Tzm;
   }
   if (gz == H.nz - 1) {
@@ -235,13 +238,13 @@ __device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc,
     const float ddx = x - xl, ddy = y - yl;
     const float beam = P * H.beam_coef * expf(-(ddx * ddx + ddy * ddy) * H.two_over_r2);
     const float q = heat_robin(H, (Tc + Tzp) * 0.5f) - beam;
-    Tzp = Tc - (q / k) * H.dz;
+    Tzp = Tc - q * rk * H.dz;
     Tg_out[idx + sz] = Tzp;
   }
-  const float txx = (Txm - 2.f * Tc + Txp) / H.dx2;  // gamma.py:49-51
-  const float tyy = (Tym - 2.f * Tc + Typ) / H.dy2;
-  const float tzz = (Tzm - 2.f * Tc + Tzp) / H.dz2;
-  return Tc + dt * ((k / H.rho / cp) * (txx + tyy + tzz));
+  const float txx = (Txm - 2.f * Tc + Txp) * H.rdx2;  // gamma.py:49-51
+  const float tyy = (Tym - 2.f * Tc + Typ) * H.rdy2;
+  const float tzz = (Tzm - 2.f * Tc + Tzp) * H.rdz2;
+  return Tc + dt * (__fdividef(k * H.inv_rho, cp) * (txx + tyy + tzz));
 }
 
 HeatConsts make_heat_consts(const pfg_heat_params& h);

@@ -34,6 +34,7 @@ struct StepArgs {
 
 
 struct TilePlan;
+int set_tune(int key, int value);
 // Warp-per-cells kernel (pf_fast.cu).
 bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
                      TilePlan* out);
