@@ -223,6 +223,29 @@ int pfg_pf_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_
                 const int32_t* argmax0, int32_t* argmax_out,
                 void* scratch, int64_t scratch_bytes, pfg_diag* out, void* stream);
 
+/* ---- diagnostics without allocation -------------------------------------
+ * No counterpart in the reference.  The same results as pfg_pf_diag for
+ * callers that can neither call cudaMalloc nor pass a scratch buffer: a host
+ * framework that owns all device memory and gives a plugin only the buffers
+ * it planned in advance (for example an XLA custom call), or a fixed-budget
+ * real-time loop.  The per-block partial sums live in a static device array
+ * of PFG_DIAG_NOALLOC_RECORDS records (165,760 bytes) that every GPU loading
+ * the library holds until the process exits.
+ *  - The first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture.
+ *  - Every call on a device shares the one array: calls whose work overlaps
+ *    on the GPU (different streams, no ordering between them) race and give
+ *    wrong results.  Order them on one stream or with events.
+ *  - A parameter set whose reduction needs more records than the array holds
+ *    returns PFG_ERR_CAPACITY (the reduction uses at most 296 blocks, so any
+ *    grid size fits today).
+ * Inputs and outputs are as for pfg_pf_diag; the caller still owns them. */
+#define PFG_DIAG_NOALLOC_RECORDS 296
+int pfg_pf_diag_noalloc(const pfg_pf_params* p, const float* eta, const float* T, int T_ghosted,
+                        const int32_t* argmax0, int32_t* argmax_out, pfg_diag* out,
+                        void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -88,6 +88,7 @@ _PROTOS = {
     "pfg_pf_diag_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(PfParams)]),
     "pfg_pf_diag": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, ctypes.c_int64, _P,
                          _P]),
+    "pfg_pf_diag_noalloc": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, _P]),
 }
 _STRUCTS = [(0, PfParams), (1, Segment), (2, HeatParams), (3, Clock), (4, Diag), (5, Quench)]
 

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <mutex>
 
 #include "pfg_device.cuh"
 #include "pfg_host.h"
@@ -242,5 +243,66 @@ extern "C" int pfg_pf_diag(const pfg_pf_params* p, const float* eta, const float
   if (scratch_bytes < pfg_pf_diag_scratch_bytes(p)) return PFG_ERR_CAPACITY;
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
   return launch_diag(p, eta, T, T_ghosted, argmax0, argmax_out, scratch, out,
+                     static_cast<cudaStream_t>(stream));
+}
+
+// ---------------------------------------------------------------------------
+// Diagnostics that allocate nothing.
+//
+// Some callers cannot hand this library a scratch buffer or let it call
+// cudaMalloc: a host framework that owns all device memory and gives a plugin
+// only the buffers it planned ahead of time (an XLA custom call, a fixed
+// arena in a real-time control loop), or a binding from a language that has
+// no CUDA allocator.  pfg_pf_diag_noalloc keeps the per-block partial records
+// in the file-scope array below instead.  It holds PFG_DIAG_NOALLOC_RECORDS
+// records (165,760 bytes); every GPU that loads the library keeps it until the
+// process exits.
+// ---------------------------------------------------------------------------
+namespace pfg {
+
+static_assert(PFG_DIAG_NOALLOC_RECORDS >= kDiagBlocks,
+              "the static array must hold the partials of the largest reduction");
+static __device__ __align__(256) DiagPartial g_diag_noalloc_partials[PFG_DIAG_NOALLOC_RECORDS];
+
+// Device address of g_diag_noalloc_partials on the current device, looked up
+// once per device (in host code the symbol name is only a host-side handle).
+static int noalloc_partials(void** out) {
+  static void* addr[64] = {nullptr};
+  static std::mutex mu;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return record_cuda(e);
+  if (dev < 0 || dev >= 64) return PFG_ERR_NO_DEVICE;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_diag_noalloc_partials);
+    if (e != cudaSuccess) return record_cuda(e);
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return PFG_OK;
+}
+
+}  // namespace pfg
+
+extern "C" int pfg_pf_diag_noalloc(const pfg_pf_params* p, const float* eta, const float* T,
+                                   int T_ghosted, const int32_t* argmax0, int32_t* argmax_out,
+                                   pfg_diag* out, void* stream) {
+  int st = check_pf_params(p);
+  if (st) return st;
+  if (!eta || !T || !out) return PFG_ERR_NULL;
+  // every block of the reduction writes one record; they must all fit
+  if ((int64_t)diag_blocks(*p) * (int64_t)sizeof(DiagPartial) >
+      (int64_t)sizeof(g_diag_noalloc_partials))
+    return PFG_ERR_CAPACITY;
+  if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  void* partials = nullptr;
+  st = noalloc_partials(&partials);
+  if (st) return st;
+  // each block overwrites its whole record before the finishing kernel reads
+  // it, and records past this call's block count are never read, so nothing
+  // left over from an earlier call needs clearing
+  return launch_diag(p, eta, T, T_ghosted, argmax0, argmax_out, partials, out,
                      static_cast<cudaStream_t>(stream));
 }
