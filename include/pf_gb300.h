@@ -145,14 +145,23 @@ const char* pfg_status_string(int status);
 const char* pfg_last_cuda_error(void);
 /* sizeof() of the ABI structs, so bindings can check their mirrors:
  * 0 pfg_pf_params, 1 pfg_segment, 2 pfg_heat_params, 3 pfg_clock, 4 pfg_diag,
- * 5 pfg_quench. */
+ * 5 pfg_quench, 6 pfg_batch_job. */
 int64_t pfg_struct_size(int which);
 
-/* Kernel selection for the stencil steps: 0 (default) uses the warp-per-cells
- * kernel whenever num_oris / VEC <= 32 (VEC = 4, 2 or 1: the largest width
- * dividing num_oris) and the generic kernel otherwise; 1 always uses the
- * generic kernel.  Both compute the same update.  Process-wide setting. */
+/* Kernel selection for the stencil steps (process-wide; all compute the same
+ * update):
+ *  0 (default) the TMA-fed kernel when num_oris % 4 == 0, else the
+ *    cp.async warp-per-cells kernel when num_oris / VEC <= 32 (VEC = 4, 2 or
+ *    1: the largest width dividing num_oris), else the generic kernel;
+ *  1 always the generic kernel;
+ *  2 the cp.async warp-per-cells kernel where it applies, else generic;
+ *  3 the same order as 0. */
 int pfg_set_kernel_variant(int variant);
+
+/* The device error flag: 0, or PFG_ERR_TIMEOUT once a bounded device-side
+ * wait of a stencil kernel ran out (the kernel then stopped early and its
+ * output is invalid).  Synchronises with the device.  clear != 0 resets it. */
+int pfg_device_error(int clear);
 
 /* Tile-plan overrides of the warp-per-cells kernel for tuning sweeps
  * (value 0 restores the automatic choice): key 0 = warps along x (1, 2, 4, 8),
@@ -161,9 +170,10 @@ int pfg_set_kernel_variant(int variant);
 int pfg_tune(int key, int value);
 
 /* The launch plan a step with these parameters would use on the current
- * device, as 12 int32: kernel (0 warp-per-cells, 1 generic), VEC, lanes per
+ * device, as 12 int32: kernel, VEC, lanes per
  * cell, tile x, tile y, warps along x, rows per warp, plane slots, planes per
- * unit, CTAs, dynamic shared memory bytes, SM count. */
+ * unit, CTAs, dynamic shared memory bytes, SM count.  kernel: 1 generic,
+ * 2 cp.async warp-per-cells, 3 TMA-fed. */
 int pfg_describe_plan(const pfg_pf_params* p, int32_t* out);
 
 /* ---- phase field --------------------------------------------------------
@@ -206,6 +216,43 @@ int pfg_heat_pf_step(const pfg_pf_params* p, const pfg_heat_params* h,
                      const float* Tg_in, float* Tg_out,
                      const pfg_clock* clk_in, pfg_clock* clk_out,
                      float dt, void* stream);
+
+/* ---- batched serving ------------------------------------------------------
+ * Many independent directional-solidification solves (each with its own
+ * grid, orientation count, parameters and step count) advanced together: one
+ * pfg_batch_step launch advances every active job by one step, so a CUDA
+ * graph of K launches (k = 0 .. K-1) replayed from the host advances all of
+ * them by K steps.  No counterpart in the reference, which solves one
+ * polycrystal per Python process (applications/phase_field/solidification/
+ * example.py:63-90); each job's step is the reference's stepper with the
+ * driver's moving gradient (pfg_pf_step_quench). */
+typedef struct pfg_batch_job {
+  pfg_pf_params params;  /* grid and physics of this job */
+  pfg_quench quench;     /* its moving temperature gradient */
+  float* eta[2];         /* device double buffer, each (nz, ny, nx, num_oris) */
+  double t0;             /* simulation time at step 0 */
+  float dt;              /* explicit Euler step */
+  int32_t reserved;
+  int64_t base_step;     /* steps completed before launch k = 0 of the next replay */
+  int64_t target_steps;  /* the job's total step count */
+} pfg_batch_job;
+
+/* Bytes of an encoded table for num_jobs jobs (host and device copies). */
+int64_t pfg_batch_table_bytes(int num_jobs);
+/* Encode jobs into `table` (host memory, table_bytes long); the caller then
+ * copies it to a device buffer of the same size.  total_units receives the
+ * number of work units (CTA tasks) of one batched step. */
+int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* table, int64_t table_bytes,
+                     int64_t* total_units);
+/* Launch k of a replay: every job with base_step + k < target_steps takes
+ * one step from eta[(base_step + k) & 1] into the other buffer, at time
+ * t0 + (base_step + k) dt.  device_table: the encoded table in device
+ * memory.  The grid is fixed (persistent CTAs), so the launch can be captured
+ * once and replayed while the table's contents change. */
+int pfg_batch_step(const void* device_table, int k, void* stream);
+/* Add k_steps to every job's base_step in the device table (the end of a
+ * replay of k_steps launches), so replays need no host-side table writes. */
+int pfg_batch_advance(void* device_table, int k_steps, void* stream);
 
 /* ---- diagnostics ----------------------------------------------------------
  * The metrics PFSolver.inspect_sol prints (allen_cahn.py:165-180) plus the

@@ -61,6 +61,12 @@ class Quench(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in ("T_base", "grad", "vel", "z0", "z_first")]
 
 
+class BatchJob(ctypes.Structure):
+    _fields_ = [("params", PfParams), ("quench", Quench), ("eta", ctypes.c_void_p * 2),
+                ("t0", ctypes.c_double), ("dt", ctypes.c_float), ("reserved", ctypes.c_int32),
+                ("base_step", ctypes.c_int64), ("target_steps", ctypes.c_int64)]
+
+
 class Diag(ctypes.Structure):
     _fields_ = [("energy", ctypes.c_double), ("max_T", ctypes.c_double),
                 ("n_cells", ctypes.c_int64), ("n_ori_changed", ctypes.c_int64),
@@ -77,6 +83,7 @@ _PROTOS = {
     "pfg_last_cuda_error": (ctypes.c_char_p, []),
     "pfg_struct_size": (ctypes.c_int64, [_I]),
     "pfg_set_kernel_variant": (_I, [_I]),
+    "pfg_device_error": (_I, [_I]),
     "pfg_tune": (_I, [_I, _I]),
     "pfg_describe_plan": (_I, [ctypes.POINTER(PfParams), _P]),
     "pfg_pf_step": (_I, [ctypes.POINTER(PfParams), _P, _P, _P, _F, _P]),
@@ -85,12 +92,18 @@ _PROTOS = {
     "pfg_heat_step": (_I, [ctypes.POINTER(HeatParams), _P, _P, _F, _F, _F, _F, _P]),
     "pfg_heat_pf_step": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(HeatParams), _P, _P, _P,
                               _P, _P, _P, _F, _P]),
+    "pfg_batch_table_bytes": (ctypes.c_int64, [_I]),
+    "pfg_batch_encode": (_I, [ctypes.POINTER(BatchJob), _I, _P, ctypes.c_int64,
+                              ctypes.POINTER(ctypes.c_int64)]),
+    "pfg_batch_step": (_I, [_P, _I, _P]),
+    "pfg_batch_advance": (_I, [_P, _I, _P]),
     "pfg_pf_diag_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(PfParams)]),
     "pfg_pf_diag": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, ctypes.c_int64, _P,
                          _P]),
     "pfg_pf_diag_noalloc": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, _P]),
 }
-_STRUCTS = [(0, PfParams), (1, Segment), (2, HeatParams), (3, Clock), (4, Diag), (5, Quench)]
+_STRUCTS = [(0, PfParams), (1, Segment), (2, HeatParams), (3, Clock), (4, Diag), (5, Quench),
+            (6, BatchJob)]
 
 _lib = None
 
@@ -151,3 +164,12 @@ def describe_plan(params):
     out = (ctypes.c_int32 * 12)()
     check(load().pfg_describe_plan(ctypes.byref(params), out), "pfg_describe_plan")
     return dict(zip(PLAN_FIELDS, list(out)))
+
+
+def device_error(clear=True):
+    """0, or PFG_ERR_TIMEOUT (6) if a bounded device-side wait ran out since
+    the last call (the affected step's output is invalid)."""
+    v = load().pfg_device_error(int(clear))
+    if v < 0 or v in (5, 8):
+        check(v if v > 0 else 5, "pfg_device_error")
+    return v

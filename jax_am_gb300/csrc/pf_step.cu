@@ -365,7 +365,12 @@ static cudaError_t launch_a(const StepArgs& a, const TilePlan& t, cudaStream_t s
   return (a.pc.aniso > 0.f) ? launch_v<true, TSRC>(a, t, s) : launch_v<false, TSRC>(a, t, s);
 }
 
+void fill_step_args(StepArgs& a, const pfg_pf_params& p, const TilePlan& t, float dt);
 static void fill_common(StepArgs& a, const pfg_pf_params& p, const TilePlan& t, float dt) {
+  fill_step_args(a, p, t, dt);
+}
+
+void fill_step_args(StepArgs& a, const pfg_pf_params& p, const TilePlan& t, float dt) {
   a.nx = p.nx; a.ny = p.ny; a.nz = p.nz; a.n = p.num_oris;
   a.bcx = p.bc_x; a.bcy = p.bc_y; a.bcz = p.bc_z;
   a.dt = dt;
@@ -413,7 +418,14 @@ template <int TSRC>
 static cudaError_t dispatch(StepArgs& a, const pfg_pf_params& p, float dt, cudaStream_t s) {
   const DeviceInfo& d = device_info();
   TilePlan t;
-  if (g_kernel_variant == 0 &&
+  const int v = g_kernel_variant;
+  if ((v == 0 || v == 3) &&
+      plan_tma_tiles(p.nx, p.ny, p.nz, p.num_oris, d.sm_count, d.smem_per_sm, &t)) {
+    fill_common(a, p, t, dt);
+    a.cpw = t.cpw; a.wx = t.wx; a.rpw = t.rpw;
+    return launch_tma_kernel<TSRC>(a, t, s);
+  }
+  if ((v == 0 || v == 2 || v == 3) &&
       plan_warp_tiles(p.nx, p.ny, p.nz, p.num_oris, d.sm_count, d.smem_per_sm, &t)) {
     fill_common(a, p, t, dt);
     a.cpw = t.cpw; a.wx = t.wx; a.rpw = t.rpw;
@@ -437,9 +449,15 @@ extern "C" int pfg_describe_plan(const pfg_pf_params* p, int32_t* out) {
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
   const DeviceInfo& d = device_info();
   TilePlan t;
-  int kernel = 0;
-  if (!(g_kernel_variant == 0 &&
-        plan_warp_tiles(p->nx, p->ny, p->nz, p->num_oris, d.sm_count, d.smem_per_sm, &t))) {
+  int kernel;
+  const int variant = g_kernel_variant;
+  if ((variant == 0 || variant == 3) &&
+      plan_tma_tiles(p->nx, p->ny, p->nz, p->num_oris, d.sm_count, d.smem_per_sm, &t)) {
+    kernel = 3;
+  } else if ((variant == 0 || variant == 2 || variant == 3) &&
+             plan_warp_tiles(p->nx, p->ny, p->nz, p->num_oris, d.sm_count, d.smem_per_sm, &t)) {
+    kernel = 2;
+  } else {
     t = plan_for_current_device(*p);
     kernel = 1;
     t.wx = 0; t.rpw = 0;
@@ -450,8 +468,14 @@ extern "C" int pfg_describe_plan(const pfg_pf_params* p, int32_t* out) {
   return PFG_OK;
 }
 
+extern "C" int pfg_device_error(int clear) {
+  if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  const int v = read_device_error(clear);
+  return v;
+}
+
 extern "C" int pfg_set_kernel_variant(int variant) {
-  if (variant != 0 && variant != 1) return PFG_ERR_PARAM;
+  if (variant < 0 || variant > 3) return PFG_ERR_PARAM;
   g_kernel_variant = variant;
   return PFG_OK;
 }

@@ -124,6 +124,27 @@ __device__ __forceinline__ TempCoef temp_coefficients(const PFConsts& c, float T
   return r;
 }
 
+// The same coefficients for the fast kernel, with cheaper arithmetic:
+//  * zeta = (1 - tanh(1e10 x)) / 2 with x = Tc / T_liq - 1 rounded to float32.
+//    Tc / T_liq is a float32, so x is 0 or at least 2^-24 in magnitude, and
+//    1e10 |x| >= 596: the float32 tanh is exactly +-1 unless x == 0.  zeta is
+//    therefore 0 (x > 0), 1 (x < 0) or 1/2 (x == 0), and NaN propagates.
+//  * Lg uses the fast exponential (relative error ~1e-6 at the Arrhenius
+//    arguments of this model, |Qg / (R T)| <= 60).
+__device__ __forceinline__ TempCoef temp_coefficients_fast(const PFConsts& c, float T, float dt) {
+  const float Tc = (T > 2000.f) ? 2000.f : T;
+  const float x = Tc / c.T_liq - 1.f;
+  const float zeta = (x > 0.f) ? 0.f : (x < 0.f) ? 1.f : (x == 0.f) ? 0.5f : x;
+  const float Lg = c.L0 * __expf(__fdividef(c.neg_Qg_over_R, Tc));
+  const float om = 1.f - zeta;
+  TempCoef r;
+  r.cg = -dt * Lg * c.mg_ad;
+  r.cl = dt * Lg * c.kappa_ad;
+  r.om2 = 2.f * om * om;
+  r.liquid = (c.force && T > c.liquid_limit) ? 1.f : 0.f;
+  return r;
+}
+
 __device__ __forceinline__ CellCoef cell_coefficients(const TempCoef& t, float S) {
   CellCoef r;
   r.cg = t.cg;

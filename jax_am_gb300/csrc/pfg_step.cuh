@@ -8,7 +8,7 @@ namespace pfg {
 // Where the phase field takes its temperature from.
 enum TSource { kTArray = 0, kTHeat = 1, kTQuench = 2 };
 
-struct StepArgs {
+struct __align__(16) StepArgs {
   int nx, ny, nz, n;
   int bcx, bcy, bcz;
   float dt;
@@ -38,7 +38,18 @@ int set_tune(int key, int value);
 // Warp-per-cells kernel (pf_fast.cu).
 bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
                      TilePlan* out);
+bool plan_warp_tiles_budget(int nx, int ny, int nz, int n, int sm_count, size_t budget,
+                            TilePlan* out);
 template <int TSRC>
 cudaError_t launch_warp_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);
+void fill_step_args(StepArgs& a, const pfg_pf_params& p, const TilePlan& t, float dt);
+// TMA-fed kernel (pf_tma.cu), num_oris % 4 == 0.
+bool plan_tma_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
+                    TilePlan* out);
+template <int TSRC>
+cudaError_t launch_tma_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);
+// The device error flag (PFG_ERR_TIMEOUT after a bounded wait ran out), or a
+// negative pfg_status if it cannot be read; clear != 0 resets it.
+int read_device_error(int clear);
 
 }  // namespace pfg

@@ -105,13 +105,14 @@ def _laser_fn(path):
     return laser
 
 
-@pytest.fixture(params=[0, 1], ids=["warp", "generic"])
+@pytest.fixture(params=[0, 1, 2], ids=["auto", "generic", "warp_cpasync"])
 def variant(request):
     from jax_am_gb300 import _lib
     lib = _lib.load()
     assert lib.pfg_set_kernel_variant(request.param) == 0
     yield request.param
     lib.pfg_set_kernel_variant(0)
+    assert _lib.device_error() == 0, "a bounded device-side wait ran out"
 
 
 @pytest.mark.parametrize("shape,n,aniso,steps", [((12, 10, 8), 5, 0.15, 6),

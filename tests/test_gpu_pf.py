@@ -25,7 +25,7 @@ def _built():
     _build.build()
 
 
-@pytest.fixture(params=[0, 1], ids=["warp", "generic"])
+@pytest.fixture(params=[0, 1, 2], ids=["auto", "generic", "warp_cpasync"])
 def variant(request):
     """Run a test on the warp-per-cells kernel and on the generic kernel."""
     from jax_am_gb300 import _lib
@@ -33,6 +33,7 @@ def variant(request):
     assert lib.pfg_set_kernel_variant(request.param) == 0
     yield request.param
     lib.pfg_set_kernel_variant(0)
+    assert _lib.device_error() == 0, "a bounded device-side wait ran out"
 
 
 def _solver(pf_args, poly):
@@ -214,7 +215,8 @@ def test_liquid_decay_rate():
     np.testing.assert_allclose(got, np.tile(got[0], (64, 1)), atol=0)
 
 
-@pytest.mark.parametrize("n,aniso", [(20, 0.15), (10, 0.15), (30, 0.0), (7, 0.15)])
+@pytest.mark.parametrize("n,aniso", [(20, 0.15), (10, 0.15), (30, 0.0), (7, 0.15), (8, 0.15),
+                                     (64, 0.0)])
 def test_warp_and_generic_kernels_agree(n, aniso):
     """Both kernels compute the same update; they differ only in float32
     rounding (packed FMAs, approximate reciprocal in the anisotropy)."""
@@ -222,9 +224,24 @@ def test_warp_and_generic_kernels_agree(n, aniso):
     lib = _lib.load()
     poly, eta, T, pf_args, oargs, obc = pf_case((41, 29, 13), n, aniso, seed=n)
     outs = []
-    for v in (0, 1):
+    for v in (0, 1, 2):
         lib.pfg_set_kernel_variant(v)
         s = _solver(pf_args, poly)
         outs.append(_run_gpu(s, eta, T, 1e-8, 4))
     lib.pfg_set_kernel_variant(0)
     assert np.abs(outs[0] - outs[1]).max() <= 1e-5
+    assert np.abs(outs[2] - outs[1]).max() <= 1e-5
+    assert _lib.device_error() == 0
+
+
+def test_plans_report_the_kernel_used():
+    from jax_am_gb300 import _lib
+    from jax_am_gb300.phase_field.allen_cahn import make_pf_params
+    lib = _lib.load()
+    for n, kernel in ((20, 3), (12, 3), (10, 2), (30, 2), (7, 2), (33, 1)):
+        poly, eta, T, pf_args, _, _ = pf_case((30, 20, 10), n, 0.15, seed=n)
+        plan = _lib.describe_plan(make_pf_params(pf_args, poly))
+        assert plan["kernel"] == kernel, (n, plan)
+    lib.pfg_set_kernel_variant(1)
+    assert _lib.describe_plan(make_pf_params(pf_args, poly))["kernel"] == 1
+    lib.pfg_set_kernel_variant(0)
