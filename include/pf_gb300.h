@@ -164,9 +164,11 @@ int pfg_set_kernel_variant(int variant);
 int pfg_device_error(int clear);
 
 /* Tile-plan overrides of the warp-per-cells kernel for tuning sweeps
- * (value 0 restores the automatic choice): key 0 = warps along x (1, 2, 4, 8),
+ * (value 0 restores the automatic choice): key 0 = warps along x (1 .. 16),
  * 1 = rows per warp (1..32), 2 = shared-memory plane slots (4..6),
- * 3 = z chunks per tile column.  Process-wide; results do not change. */
+ * 3 = z chunks per tile column, 5 = consumer threads of the TMA-fed kernel
+ * (256: two CTAs per SM; 512: one larger CTA per SM).  Process-wide; results
+ * do not change. */
 int pfg_tune(int key, int value);
 
 /* The launch plan a step with these parameters would use on the current

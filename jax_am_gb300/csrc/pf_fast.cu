@@ -44,19 +44,23 @@ __global__ void __launch_bounds__(kThreads, 2) pf_warp_kernel(const __grid_const
 // host side
 // ---------------------------------------------------------------------------
 
+extern int g_tma_consumers;
 // Plan overrides for tuning sweeps (0 = automatic).
 static int g_tune_wx = 0, g_tune_rpw = 0, g_tune_stages = 0, g_tune_zchunks = 0;
 
 int set_tune(int key, int value) {
   if (value < 0) return PFG_ERR_PARAM;
   switch (key) {
-    case 0: if (value && value != 1 && value != 2 && value != 4 && value != 8) return PFG_ERR_PARAM;
+    case 0: if (value && value != 1 && value != 2 && value != 4 && value != 8 && value != 16)
+              return PFG_ERR_PARAM;
             g_tune_wx = value; return PFG_OK;
     case 1: if (value > 32) return PFG_ERR_PARAM;
             g_tune_rpw = value; return PFG_OK;
     case 2: if (value && (value < 4 || value > 6)) return PFG_ERR_PARAM;
             g_tune_stages = value; return PFG_OK;
     case 3: g_tune_zchunks = value; return PFG_OK;
+    case 5: if (value && value != 256 && value != 512) return PFG_ERR_PARAM;
+            g_tma_consumers = value ? value : 256; return PFG_OK;
     default: return PFG_ERR_PARAM;
   }
 }
@@ -69,17 +73,24 @@ bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
 
 bool plan_warp_tiles_budget(int nx, int ny, int nz, int n, int sm_count, size_t budget,
                             TilePlan* out) {
+  return plan_warp_tiles_ex(nx, ny, nz, n, sm_count, budget, 8, 2, 1 << 30, out);
+}
+
+// warps: warps that own cells (the tile is wx * cpw by (warps / wx) * rpw cells);
+// ctas_per_sm: for the wave count; max_cells: cap on tile cells.
+bool plan_warp_tiles_ex(int nx, int ny, int nz, int n, int sm_count, size_t budget, int warps,
+                        int ctas_per_sm, int max_cells, TilePlan* out) {
   TilePlan t{};
   t.vec = vec_width(n);
   t.tpc = n / t.vec;
   if (t.tpc > 32) return false;
   t.cpw = 32 / t.tpc;
   t.stages = g_tune_stages ? g_tune_stages : 4;
-  const long concurrent = 2L * sm_count;
+  const long concurrent = (long)ctas_per_sm * sm_count;
   double best = 1e30;
-  for (int wx = 1; wx <= 8; wx *= 2) {
+  for (int wx = 1; wx <= warps; wx *= 2) {
     if (g_tune_wx && wx != g_tune_wx) continue;
-    const int wy = 8 / wx;
+    const int wy = warps / wx;
     const int tx = wx * t.cpw;
     if (!g_tune_wx && wx > 1 && (wx / 2) * t.cpw >= nx) continue;  // a narrower tile covers x
     for (int rpw = 1; rpw <= 32; ++rpw) {
@@ -90,7 +101,7 @@ bool plan_warp_tiles_budget(int nx, int ny, int nz, int n, int sm_count, size_t 
       const int tslot = ((ty + 2) * (tx + 2) + 3) / 4 * 4;
       const size_t smem = (size_t)t.stages * ((size_t)(ty + 2) * pitch + tslot) * 4 +
                           (size_t)2 * ty * tx * 16;
-      if (smem > budget) break;
+      if (smem > budget || tx * ty > max_cells) break;
       const long tiles = (long)((nx + tx - 1) / tx) * ((ny + ty - 1) / ty);
       const double cover = (double)tiles * tx * ty / ((double)nx * ny);
       const double halo = (double)(tx + 2) * (ty + 2) / ((double)tx * ty);
@@ -100,9 +111,11 @@ bool plan_warp_tiles_budget(int nx, int ny, int nz, int n, int sm_count, size_t 
       const long zc = (nz + zch - 1) / zch;
       const double waves = (double)(tiles * ((nz + zc - 1) / zc)) / (double)concurrent;
       const double wave_eff = waves / std::ceil(waves);
-      // measured on GB300: per-plane staging and barrier costs make the halo
-      // ratio count about quadratically
-      const double score = cover * halo * halo / wave_eff;
+      // measured on GB300: halo columns cost about twice what halo rows cost
+      // (every staged row carries its two x-halo cells)
+      const double hx = (double)(tx + 2) / tx, hy = (double)(ty + 2) / ty;
+      const double score = cover * hx * hx * hy / wave_eff;
+      (void)halo;
       if (score < best - 1e-9) {
         best = score;
         t.tx = tx; t.ty = ty; t.wx = wx; t.rpw = rpw;

@@ -208,7 +208,7 @@ pf_zmarch_kernel(const __grid_constant__ StepArgs a) {
         const int64_t idx = (int64_t)(z + 1) * sz + (int64_t)(gy + 1) * sy + gx + 1;
         const float Tn = heat_cell_update(a.hc, Tc, t_cur[o - 1], t_cur[o + 1], t_cur[o - tp],
                                           t_cur[o + tp], t_prev[o], t_next[o], gx, gy, z, xl, yl,
-                                          P, a.dt, a.T_out, idx, 1, sy, sz);
+                                          P, a.dt, a.T_out, idx, (int64_t)1, sy, sz);
         a.T_out[idx] = Tn;
       }
     }

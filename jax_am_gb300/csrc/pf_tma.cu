@@ -1,16 +1,18 @@
 // TMA-fed phase-field step: the fast path when num_oris is a multiple of 4.
 //
-// Same tiling and arithmetic as pf_fast.cu (warps own whole cells, per-cell
-// coefficients one plane ahead, folded element update), with the staging
-// moved to a producer warp:
-//  * Each halo row of a plane tile is one contiguous run of cells in HBM; the
-//    producer copies it into shared memory with one cp.async.bulk (TMA)
-//    transfer that completes on the slot's "full" mbarrier (expect-tx bytes).
-//    The temperature tile (4-byte cells, unaligned rows) goes through
-//    ordinary cp.async copies that arrive on the same barrier.
-//  * The eight consumer warps wait on "full", release the slot on "empty"
-//    after their last use of the plane, and synchronise among themselves
-//    with a named barrier only for the per-cell coefficient buffer.
+// Same tiling and arithmetic as the warp-per-cells kernel (warps own whole
+// cells, per-cell coefficients one plane ahead, folded element update), with
+// the staging done by the Tensor Memory Accelerator:
+//  * Each halo row of a plane tile is one contiguous run of cells in HBM and
+//    is copied into shared memory by one cp.async.bulk (TMA) transfer that
+//    completes on the slot's mbarrier (expect-tx bytes).  The temperature
+//    tile (4-byte cells, unaligned rows) goes through ordinary cp.async copies
+//    that arrive on the same barrier.
+//  * All threads compute; after the per-plane barrier (which every thread
+//    passes anyway for the coefficient buffer) warp 0 issues the copies of
+//    the plane S-1 ahead into the slot everyone has just finished with, so no
+//    producer warp and no "empty" barriers are needed and the CTA keeps the
+//    full register budget (16 warps per SM).
 //  * Neumann halo cells along x are never copied: the stencil offset of the
 //    edge cell points at itself.  Periodic halo cells are copied by TMA.
 // Every wait is bounded (about one second of clock64 cycles); a wait that
@@ -28,8 +30,6 @@ namespace pfg {
 
 __device__ int g_pfg_device_error = 0;  // PFG_ERR_TIMEOUT once a bounded wait ran out
 
-constexpr int kConsumers = 256;                 // eight consumer warps
-constexpr int kTmaThreads = kConsumers + 32;    // plus one producer warp
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
@@ -42,9 +42,6 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned by
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)),
                "r"(bytes)
                : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_addr(bar)) : "memory");
 }
 __device__ __forceinline__ void cp_async_mbar_arrive_noinc(uint64_t* bar) {
   asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" ::"r"(smem_addr(bar))
@@ -80,9 +77,6 @@ __device__ __forceinline__ void tma_row(void* dst, const void* src, unsigned byt
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
-__device__ __forceinline__ void consumer_sync() {
-  asm volatile("bar.sync 1, %0;\n" ::"n"(kConsumers) : "memory");
-}
 
 // Folded update of one element (see pf_fast.cu for the derivation).
 struct LapConstsT {
@@ -101,7 +95,9 @@ __device__ __forceinline__ float tma_update_elem(const LapConstsT& L, float e, f
     const float p1 = fmaf(d[3], ex, fmaf(d[4], ey, d[5] * ez));
     const float q0 = p0 * p0, q1 = p1 * p1;
     const float q2 = ee - q0 - q1;
-    const float c2 = fminf(fmaxf(fmaxf(q0, q1), q2) * __fdividef(1.f, ee), 1.f);
+    float m;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(q0), "f"(q1), "f"(q2));
+    const float c2 = fminf(m * rcp_approx(ee), 1.f);
     u = fmaf(k.w, fmaf(-c2, c2, c2), k.z);
   }
   return fmaf(u, lap, e * fmaf(k.y, e * e, k.x));
@@ -114,8 +110,11 @@ __device__ __forceinline__ float4 tma_fold(const PFConsts& c, const TempCoef& tc
   return make_float4(1.f + tc.cg * K, -3.f * tc.cg, clw * (1.f + c.aniso), -2.f * c.aniso * clw);
 }
 
-template <bool ANISO, int TSRC>
-__global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_constant__ StepArgs a) {
+// NC threads (256: two CTAs per SM, or 512: one CTA per SM with a tile
+// twice as large).
+template <bool ANISO, int TSRC, int NC>
+__global__ void __launch_bounds__(NC, NC == 256 ? 2 : 1)
+pf_tma_kernel(const __grid_constant__ StepArgs a) {
   constexpr int VEC = 4;
   extern __shared__ __align__(128) float smem[];
   const int S = a.stages;
@@ -124,7 +123,6 @@ __global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_con
   float* T_s = eta_s + (size_t)S * slot_floats;
   float4* cc = reinterpret_cast<float4*>(T_s + (size_t)S * a.tslot);  // [2][ty * tx]
   uint64_t* full = reinterpret_cast<uint64_t*>(cc + 2 * a.ty * a.tx);
-  uint64_t* empty = full + S;
 
   // ---- work unit
   const int per_plane = a.tiles_x * a.tiles_y;
@@ -140,13 +138,11 @@ __global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_con
   const int nplanes = ze - zb + 2;  // planes zb-1 .. ze
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  __shared__ int s_abort;  // set by any consumer whose wait ran out; read after a barrier
+  __shared__ int s_abort;  // set by any thread whose wait ran out; read after a barrier
   if (threadIdx.x == 0) {
     s_abort = 0;
-    for (int s = 0; s < S; ++s) {
-      mbar_init(&full[s], 1 + 32);  // producer's expect-tx arrival + 32 cp.async arrivals
-      mbar_init(&empty[s], kConsumers / 32);
-    }
+    // expect-tx arrival of warp 0's lane 0 + one cp.async arrival per thread
+    for (int s = 0; s < S; ++s) mbar_init(&full[s], 1 + NC);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   __syncthreads();
@@ -160,25 +156,22 @@ __global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_con
     }
   }
 
-  if (warp == kConsumers / 32) {
-    // =================== producer warp ===================
-    const int cx0 = max(x0 - 1, 0), cx1 = min(xe + 1, a.nx);
-    const int dst_cell0 = cx0 - (x0 - 1);
-    const bool wrap_left = (x0 == 0) && a.bcx == PFG_BC_PERIODIC;
-    const bool wrap_right = (xe == a.nx) && a.bcx == PFG_BC_PERIODIC;
-    const int rows = tyv + 2;
-    const unsigned row_bytes = (unsigned)((cx1 - cx0) * n * 4);
-    const unsigned cell_bytes = (unsigned)(n * 4);
-    const unsigned plane_bytes =
-        (unsigned)rows * (row_bytes + (wrap_left ? cell_bytes : 0u) + (wrap_right ? cell_bytes : 0u));
-    const int tp = a.tx + 2;
-    int issued = 0;
-    bool ok = true;
-    for (int j = 0; j < nplanes && ok; ++j) {
-      const int s = j % S, k = j / S;
-      if (k > 0) ok = mbar_wait(&empty[s], (unsigned)((k - 1) & 1));
-      if (!ok) break;
-      const int pz = zb - 1 + j;
+  // ---- staging: plane j (grid plane zb - 1 + j) into slot j % S
+  const int cx0 = max(x0 - 1, 0), cx1 = min(xe + 1, a.nx);
+  const int dst_cell0 = cx0 - (x0 - 1);
+  const bool wrap_left = (x0 == 0) && a.bcx == PFG_BC_PERIODIC;
+  const bool wrap_right = (xe == a.nx) && a.bcx == PFG_BC_PERIODIC;
+  const int rows = tyv + 2;
+  const unsigned row_bytes = (unsigned)((cx1 - cx0) * n * 4);
+  const unsigned cell_bytes = (unsigned)(n * 4);
+  const unsigned plane_bytes =
+      (unsigned)rows * (row_bytes + (wrap_left ? cell_bytes : 0u) + (wrap_right ? cell_bytes : 0u));
+  const int tp = a.tx + 2;
+  const int tcols = txv + 2;
+  auto stage = [&](int j) {
+    const int s = j % S;
+    const int pz = zb - 1 + j;
+    if (warp == 0) {
       const int gz = bc_index(pz, a.nz, a.bcz);
       float* es = eta_s + (size_t)s * slot_floats;
       if (lane == 0) mbar_arrive_expect_tx(&full[s], plane_bytes);
@@ -189,40 +182,28 @@ __global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_con
         float* dst_row = es + r * a.pitch;
         tma_row(dst_row + dst_cell0 * n, src_row + (int64_t)cx0 * n, row_bytes, &full[s]);
         if (wrap_left) tma_row(dst_row, src_row + (int64_t)(a.nx - 1) * n, cell_bytes, &full[s]);
-        if (wrap_right)
-          tma_row(dst_row + (txv + 1) * n, src_row, cell_bytes, &full[s]);
+        if (wrap_right) tma_row(dst_row + (txv + 1) * n, src_row, cell_bytes, &full[s]);
       }
-      float* ts = T_s + (size_t)s * a.tslot;
-      if constexpr (TSRC == kTHeat) {
-        const int cols = txv + 2;
-        const int64_t gsy = a.nx + 2, gsz = (int64_t)(a.ny + 2) * (a.nx + 2);
-        for (int i = lane; i < rows * cols; i += 32) {
-          const int r = i / cols, c = i - r * cols;
-          cp_async<4>(ts + r * tp + c, a.T + (int64_t)(pz + 1) * gsz + (int64_t)(y0 + r) * gsy + x0 + c);
-        }
-      } else if constexpr (TSRC == kTArray) {
-        if (pz >= 0 && pz < a.nz) {
-          for (int i = lane; i < tyv * txv; i += 32) {
-            const int r = i / txv, c = i - r * txv;
-            cp_async<4>(ts + (r + 1) * tp + c + 1,
-                        a.T + ((int64_t)pz * a.ny + y0 + r) * a.nx + x0 + c);
-          }
+    }
+    float* ts = T_s + (size_t)s * a.tslot;
+    if constexpr (TSRC == kTHeat) {
+      const int64_t gsy = a.nx + 2, gsz = (int64_t)(a.ny + 2) * (a.nx + 2);
+      for (int i = threadIdx.x; i < rows * tcols; i += NC) {
+        const int r = i / tcols, c = i - r * tcols;
+        cp_async<4>(ts + r * tp + c, a.T + (int64_t)(pz + 1) * gsz + (int64_t)(y0 + r) * gsy + x0 + c);
+      }
+    } else if constexpr (TSRC == kTArray) {
+      if (pz >= 0 && pz < a.nz) {
+        for (int i = threadIdx.x; i < tyv * txv; i += NC) {
+          const int r = i / txv, c = i - r * txv;
+          cp_async<4>(ts + (r + 1) * tp + c + 1, a.T + ((int64_t)pz * a.ny + y0 + r) * a.nx + x0 + c);
         }
       }
-      cp_async_mbar_arrive_noinc(&full[s]);
-      issued = j + 1;
     }
-    // drain: every copy issued must have landed before the CTA's shared
-    // memory can be released.  Only the latest use of each slot can still be
-    // in flight (earlier uses completed before the slot was refilled), and a
-    // barrier can only be asked about its latest phase.
-    for (int j = max(0, issued - S); j < issued; ++j) {
-      if (!mbar_wait(&full[j % S], (unsigned)((j / S) & 1))) break;
-    }
-    return;
-  }
+    cp_async_mbar_arrive_noinc(&full[s]);
+  };
 
-  // =================== consumer warps ===================
+  // ---- lane -> (cell, orientation chunk)
   const int tpc = a.tpc;
   const int wxi = warp % a.wx, wyi = warp / a.wx;
   const int lc = lane / tpc, kk = lane - lc * tpc;
@@ -251,7 +232,24 @@ __global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_con
   float xl = 0.f, yl = 0.f, Pw = 0.f;
   if constexpr (TSRC == kTHeat) laser_at(a.hp, t0 + 0.5 * (double)a.dt, &xl, &yl, &Pw);
 
+  // ---- this thread's cells for the per-cell work (at most two), fixed per unit
   const int ncell = tyv * txv;
+  const int gsy = a.nx + 2, gsz = (a.ny + 2) * (a.nx + 2);  // ghosted strides (host checks < 2^31)
+  int c_eoff[2], c_toff[2], c_cc[2], c_g[2], c_hx[2], c_hy[2];
+  bool c_ok[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int i = threadIdx.x + q * NC;
+    c_ok[q] = i < ncell;
+    const int r = c_ok[q] ? i / txv : 0, c = c_ok[q] ? i - r * txv : 0;
+    c_eoff[q] = (r + 1) * a.pitch + (c + 1) * n;
+    c_toff[q] = (r + 1) * tp + c + 1;
+    c_cc[q] = r * a.tx + c;
+    c_hx[q] = x0 + c;
+    c_hy[q] = y0 + r;
+    c_g[q] = (c_hy[q] + 1) * gsy + c_hx[q] + 1;
+  }
+
   // per-cell coefficients of plane pz (in slot s) -> cc[buf]
   auto cell_coefs = [&](int s, int buf, int pz) {
     const float* es = eta_s + (size_t)s * slot_floats;
@@ -263,58 +261,66 @@ __global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_con
       const float Tz = (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t0);
       plane = temp_coefficients_fast(a.pc, Tz, a.dt);
     }
-    for (int i = threadIdx.x; i < ncell; i += kConsumers) {
-      const int r = i / txv, c = i - r * txv;
-      const float* ce = es + (r + 1) * a.pitch + (c + 1) * n;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (!c_ok[q]) continue;
+      const float* ce = es + c_eoff[q];
       float s0 = 0.f, s1 = 0.f;
-      int q = 0;
-      for (; q + 8 <= n; q += 8) {
-        const float4 u = *reinterpret_cast<const float4*>(ce + q);
-        const float4 v = *reinterpret_cast<const float4*>(ce + q + 4);
+      int k = 0;
+      for (; k + 8 <= n; k += 8) {
+        const float4 u = *reinterpret_cast<const float4*>(ce + k);
+        const float4 v = *reinterpret_cast<const float4*>(ce + k + 4);
         s0 = fmaf(u.x, u.x, fmaf(u.y, u.y, fmaf(u.z, u.z, fmaf(u.w, u.w, s0))));
         s1 = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, s1))));
       }
-      for (; q < n; q += 4) {
-        const float4 u = *reinterpret_cast<const float4*>(ce + q);
+      if (k < n) {
+        const float4 u = *reinterpret_cast<const float4*>(ce + k);
         s0 = fmaf(u.x, u.x, fmaf(u.y, u.y, fmaf(u.z, u.z, fmaf(u.w, u.w, s0))));
       }
       TempCoef tc;
       if constexpr (TSRC == kTQuench) tc = plane;
-      else tc = temp_coefficients_fast(a.pc, ts[(r + 1) * (a.tx + 2) + c + 1], a.dt);
-      cb[r * a.tx + c] = tma_fold(a.pc, tc, s0 + s1);
+      else tc = temp_coefficients_fast(a.pc, ts[c_toff[q]], a.dt);
+      cb[c_cc[q]] = tma_fold(a.pc, tc, s0 + s1);
     }
   };
 
+  // ---- prologue: planes 0 .. S-2 in flight, wait for planes 0, 1, 2
+  int issued = 0;
+  for (int j = 0; j < S - 1 && j < nplanes; ++j) { stage(j); issued = j + 1; }
   bool ok = true;
-  // prologue: planes zb-1, zb, zb+1 (slots 0, 1, 2 of their first use)
   for (int j = 0; j < 3 && ok; ++j) ok = mbar_wait(&full[j % S], (unsigned)((j / S) & 1));
   if (ok) cell_coefs(1 % S, 0, zb);
   else s_abort = 1;
 
   const int64_t plane_elems = (int64_t)a.ny * a.nx * n;
+  const int64_t row_elems = (int64_t)a.nx * n;
+  const int64_t col_base = ((int64_t)y0 * a.nx + gx) * n + i0;
+  const int r_begin = wyi * a.rpw;
+  const int r_end = min(r_begin + a.rpw, tyv);
   for (int z = zb; z < ze; ++z) {
     const int m = z - zb;
     const int j_next = m + 2;
     if (ok) ok = mbar_wait(&full[j_next % S], (unsigned)((j_next / S) & 1));
     if (!ok) *(volatile int*)&s_abort = 1;
-    consumer_sync();  // cc[m & 1] complete; everyone finished iteration m-1
-    if (*(volatile int*)&s_abort) break;  // uniform across the consumer warps
+    __syncthreads();  // cc[m & 1] complete; everyone finished iteration m-1
+    if (*(volatile int*)&s_abort) break;  // uniform across the CTA
+    // the slot of plane m-1 is free: fill it with plane m+S-1
+    if (m + S - 1 < nplanes) { stage(m + S - 1); issued = m + S; }
     const int s_prev = m % S, s_cur = (m + 1) % S, s_next = j_next % S;
 
     if constexpr (TSRC == kTHeat) {
       const float* tp_ = T_s + (size_t)s_prev * a.tslot;
       const float* tc_ = T_s + (size_t)s_cur * a.tslot;
       const float* tn_ = T_s + (size_t)s_next * a.tslot;
-      const int tp = a.tx + 2;
-      const int64_t sy = a.nx + 2, sz = (int64_t)(a.ny + 2) * (a.nx + 2);
-      for (int i = threadIdx.x; i < ncell; i += kConsumers) {
-        const int r = i / txv, c = i - r * txv;
-        const int o = (r + 1) * tp + c + 1;
-        const int hx = x0 + c, hy = y0 + r;
-        const int64_t idx = (int64_t)(z + 1) * sz + (int64_t)(hy + 1) * sy + hx + 1;
+      const int zoff = (z + 1) * gsz;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        if (!c_ok[q]) continue;
+        const int o = c_toff[q];
+        const int idx = zoff + c_g[q];
         const float Tn = heat_cell_update(a.hc, tc_[o], tc_[o - 1], tc_[o + 1], tc_[o - tp],
-                                          tc_[o + tp], tp_[o], tn_[o], hx, hy, z, xl, yl, Pw,
-                                          a.dt, a.T_out, idx, 1, sy, sz);
+                                          tc_[o + tp], tp_[o], tn_[o], c_hx[q], c_hy[q], z, xl, yl,
+                                          Pw, a.dt, a.T_out, idx, 1, gsy, gsz);
         a.T_out[idx] = Tn;
       }
     }
@@ -324,22 +330,40 @@ __global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_con
     const float* e_prev = eta_s + (size_t)s_prev * slot_floats;
     const float* e_next = eta_s + (size_t)s_next * slot_floats;
     const float4* ccb = cc + (size_t)(m & 1) * a.ty * a.tx;
-    auto row_update = [&](int r, const VecF<VEC>& c, const VecF<VEC>& xm, const VecF<VEC>& xp,
-                          const VecF<VEC>& ym, const VecF<VEC>& yp, const VecF<VEC>& zm,
-                          const VecF<VEC>& zp) {
+    float* out_row = a.eta_out + ((int64_t)z * plane_elems + col_base + (int64_t)r_begin * row_elems);
+    auto row_out = [&](int r, float* dst, const VecF<VEC>& c, const VecF<VEC>& xm,
+                       const VecF<VEC>& xp, const VecF<VEC>& ym, const VecF<VEC>& yp,
+                       const VecF<VEC>& zm, const VecF<VEC>& zp) {
       const float4 kc = ccb[r * a.tx + xs];
       VecF<VEC> out;
 #pragma unroll
       for (int v = 0; v < VEC; ++v)
         out.v[v] = tma_update_elem<ANISO>(L, c.v[v], xm.v[v], xp.v[v], ym.v[v], yp.v[v], zm.v[v],
                                           zp.v[v], &dl[ANISO ? v * 6 : 0], kc);
-      if (col_valid) {
-        const int64_t g = (int64_t)z * plane_elems + ((int64_t)(y0 + r) * a.nx + gx) * n + i0;
-        out.store(a.eta_out + g);
-      }
+      if (col_valid) out.store(dst);
     };
-    const int r_end = min(wyi * a.rpw + a.rpw, tyv);
-    for (int r = wyi * a.rpw; r < r_end; ++r) {
+    int r = r_begin;
+    // two rows at a time: rows r-1 .. r+2 of the plane are loaded once
+    for (; r + 1 < r_end; r += 2, out_row += 2 * row_elems) {
+      const int off = (r + 1) * a.pitch + (xs + 1) * n + i0;
+      const int off2 = off + a.pitch;
+      VecF<VEC> ym, c, c2, yp2, xm, xp, xm2, xp2, zm, zp, zm2, zp2;
+      ym.load(e_cur + off - a.pitch);
+      c.load(e_cur + off);
+      c2.load(e_cur + off2);
+      yp2.load(e_cur + off2 + a.pitch);
+      xm.load(e_cur + off + off_xm);
+      xp.load(e_cur + off + off_xp);
+      xm2.load(e_cur + off2 + off_xm);
+      xp2.load(e_cur + off2 + off_xp);
+      zm.load(e_prev + off);
+      zp.load(e_next + off);
+      zm2.load(e_prev + off2);
+      zp2.load(e_next + off2);
+      row_out(r, out_row, c, xm, xp, ym, c2, zm, zp);
+      row_out(r + 1, out_row + row_elems, c2, xm2, xp2, c, yp2, zm2, zp2);
+    }
+    if (r < r_end) {
       const int off = (r + 1) * a.pitch + (xs + 1) * n + i0;
       VecF<VEC> c, xm, xp, ym, yp, zm, zp;
       c.load(e_cur + off);
@@ -349,11 +373,15 @@ __global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_con
       yp.load(e_cur + off + a.pitch);
       zm.load(e_prev + off);
       zp.load(e_next + off);
-      row_update(r, c, xm, xp, ym, yp, zm, zp);
+      row_out(r, out_row, c, xm, xp, ym, yp, zm, zp);
     }
-    // plane z-1 (slot s_prev) is no longer needed by this warp
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s_prev]);
+  }
+  // drain: copies still in flight must land before the CTA's shared memory is
+  // released (in a normal run every issued plane has been waited for already)
+  cp_async_wait(0);
+  if (threadIdx.x == 0) {
+    for (int j = max(0, issued - S); j < issued; ++j)
+      if (!mbar_wait(&full[j % S], (unsigned)((j / S) & 1))) break;
   }
 }
 
@@ -361,20 +389,29 @@ __global__ void __launch_bounds__(kTmaThreads, 2) pf_tma_kernel(const __grid_con
 // host side
 // ---------------------------------------------------------------------------
 
+int g_tma_consumers = 256;  // threads per CTA: 256 (two CTAs per SM) or 512 (one per SM)
+
 bool plan_tma_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
                     TilePlan* out) {
   if (n % 4 != 0) return false;
+  // ghosted temperature offsets are 32-bit in this kernel
+  if ((int64_t)(nx + 2) * (ny + 2) * (nz + 2) >= ((int64_t)1 << 31)) return false;
   TilePlan t{};
-  if (!plan_warp_tiles(nx, ny, nz, n, sm_count, max_smem_per_sm, &t)) return false;
+  const int warps = g_tma_consumers / 32;
+  const int ctas = g_tma_consumers == 256 ? 2 : 1;
+  const size_t budget = (size_t)max_smem_per_sm / ctas - 2048 - 6 * sizeof(uint64_t) - 64;
+  if (!plan_warp_tiles_ex(nx, ny, nz, n, sm_count, budget, warps, ctas, 2 * g_tma_consumers, &t))
+    return false;
   // the ring's barriers sit after the coefficient buffer
-  t.smem += (size_t)2 * t.stages * sizeof(uint64_t);
+  t.smem += (size_t)t.stages * sizeof(uint64_t);
+  t.rs = g_tma_consumers;  // threads of this plan
   *out = t;
   return true;
 }
 
-template <bool ANISO, int TSRC>
+template <bool ANISO, int TSRC, int NC>
 static cudaError_t launch_tma_t(const StepArgs& a, const TilePlan& t, cudaStream_t s) {
-  auto k = pf_tma_kernel<ANISO, TSRC>;
+  auto k = pf_tma_kernel<ANISO, TSRC, NC>;
   static int configured[64] = {0};
   const int dev = device_info().device;
   if (dev < 0 || dev >= 64 || configured[dev] < (int)t.smem) {
@@ -383,13 +420,17 @@ static cudaError_t launch_tma_t(const StepArgs& a, const TilePlan& t, cudaStream
     if (e != cudaSuccess) return e;
     if (dev >= 0 && dev < 64) configured[dev] = (int)t.smem;
   }
-  k<<<(unsigned)t.units, kTmaThreads, t.smem, s>>>(a);
+  k<<<(unsigned)t.units, NC, t.smem, s>>>(a);
   return cudaGetLastError();
 }
 
 template <int TSRC>
 cudaError_t launch_tma_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s) {
-  return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC>(a, t, s) : launch_tma_t<false, TSRC>(a, t, s);
+  if (t.rs == 512)
+    return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 512>(a, t, s)
+                              : launch_tma_t<false, TSRC, 512>(a, t, s);
+  return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 256>(a, t, s)
+                            : launch_tma_t<false, TSRC, 256>(a, t, s);
 }
 
 template cudaError_t launch_tma_kernel<kTArray>(const StepArgs&, const TilePlan&, cudaStream_t);

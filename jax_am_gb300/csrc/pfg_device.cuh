@@ -33,6 +33,13 @@ __device__ __forceinline__ void cp_async_wait(int pending) {
   else asm volatile("cp.async.wait_group 2;\n" ::: "memory");
 }
 
+// Reciprocal to within 1 ulp (one MUFU instruction, denormal inputs flushed).
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Vector of V floats moved as one 4/8/16-byte access.
 template <int V>
 struct VecF {
@@ -135,7 +142,7 @@ __device__ __forceinline__ TempCoef temp_coefficients_fast(const PFConsts& c, fl
   const float Tc = (T > 2000.f) ? 2000.f : T;
   const float x = Tc / c.T_liq - 1.f;
   const float zeta = (x > 0.f) ? 0.f : (x < 0.f) ? 1.f : (x == 0.f) ? 0.5f : x;
-  const float Lg = c.L0 * __expf(__fdividef(c.neg_Qg_over_R, Tc));
+  const float Lg = c.L0 * __expf(c.neg_Qg_over_R * rcp_approx(Tc));
   const float om = 1.f - zeta;
   TempCoef r;
   r.cg = -dt * Lg * c.mg_ad;
@@ -220,14 +227,14 @@ __device__ __forceinline__ void laser_at(const pfg_heat_params& hp, double t, fl
 // array and sx, sy, sz its element strides.  New ghosts of the faces this cell touches
 // are computed from the old ghost and written to Tg_out (gamma.py:18-43);
 // the Laplacian uses them (gamma.py:58-60).  Returns the new interior value.
+template <typename IDX>
 __device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc, float Txm,
                                                   float Txp, float Tym, float Typ, float Tzm,
                                                   float Tzp, int gx, int gy, int gz, float xl,
                                                   float yl, float P, float dt, float* Tg_out,
-                                                  int64_t idx, int64_t sx, int64_t sy,
-                                                  int64_t sz) {
+                                                  IDX idx, IDX sx, IDX sy, IDX sz) {
   const float k = heat_k(H, Tc);
-  const float rk = __fdividef(1.f, k);
+  const float rk = rcp_approx(k);
   const float Tcl = fminf(fmaxf(Tc, H.Ts), H.Tl);
   const float fl = (Tcl - H.Ts) * H.inv_dTsl;
   const float cp = 0.2441f * fminf(fmaxf(Tc, 300.f), H.Tl) + 338.39f +
@@ -265,7 +272,7 @@ __device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc,
   const float txx = (Txm - 2.f * Tc + Txp) * H.rdx2;  // gamma.py:49-51
   const float tyy = (Tym - 2.f * Tc + Typ) * H.rdy2;
   const float tzz = (Tzm - 2.f * Tc + Tzp) * H.rdz2;
-  return Tc + dt * (__fdividef(k * H.inv_rho, cp) * (txx + tyy + tzz));
+  return Tc + dt * ((k * H.inv_rho) * rcp_approx(cp) * (txx + tyy + tzz));
 }
 
 HeatConsts make_heat_consts(const pfg_heat_params& h);

@@ -40,6 +40,8 @@ bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
                      TilePlan* out);
 bool plan_warp_tiles_budget(int nx, int ny, int nz, int n, int sm_count, size_t budget,
                             TilePlan* out);
+bool plan_warp_tiles_ex(int nx, int ny, int nz, int n, int sm_count, size_t budget, int warps,
+                        int ctas_per_sm, int max_cells, TilePlan* out);
 template <int TSRC>
 cudaError_t launch_warp_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);
 void fill_step_args(StepArgs& a, const pfg_pf_params& p, const TilePlan& t, float dt);

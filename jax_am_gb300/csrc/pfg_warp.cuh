@@ -46,7 +46,7 @@ __device__ __forceinline__ float update_elem(const LapConsts& L, float e, float 
     const float q2 = ee - q0 - q1;
     // |e| = 0 gives 0 * inf = NaN and fminf(NaN, 1) = 1: the reference's
     // NaN-angle-to-zero rule; rounding above 1 is clamped the same way
-    const float c2 = fminf(fmaxf(fmaxf(q0, q1), q2) * __fdividef(1.f, ee), 1.f);
+    const float c2 = fminf(fmaxf(fmaxf(q0, q1), q2) * rcp_approx(ee), 1.f);
     u = fmaf(k.w, fmaf(-c2, c2, c2), k.z);
   }
   return fmaf(u, lap, e * fmaf(k.y, e * e, k.x));
@@ -257,7 +257,7 @@ __device__ __forceinline__ void warp_unit(const StepArgs& a, int unit, double t0
         const int64_t idx = (int64_t)(z + 1) * sz + (int64_t)(gy + 1) * sy + gx + 1;
         const float Tn = heat_cell_update(a.hc, tc_[o], tc_[o - 1], tc_[o + 1], tc_[o - tp],
                                           tc_[o + tp], tp_[o], tn_[o], gx, gy, z, xl, yl, Pw,
-                                          a.dt, a.T_out, idx, 1, sy, sz);
+                                          a.dt, a.T_out, idx, (int64_t)1, sy, sz);
         a.T_out[idx] = Tn;
       }
     }

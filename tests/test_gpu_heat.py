@@ -105,13 +105,17 @@ def _laser_fn(path):
     return laser
 
 
-@pytest.fixture(params=[0, 1, 2], ids=["auto", "generic", "warp_cpasync"])
+@pytest.fixture(params=[0, 1, 2, 512], ids=["auto", "generic", "warp_cpasync", "tma512"])
 def variant(request):
     from jax_am_gb300 import _lib
     lib = _lib.load()
-    assert lib.pfg_set_kernel_variant(request.param) == 0
+    if request.param == 512:  # the TMA-fed kernel with one 512-thread CTA per SM
+        assert lib.pfg_set_kernel_variant(0) == 0 and lib.pfg_tune(5, 512) == 0
+    else:
+        assert lib.pfg_set_kernel_variant(request.param) == 0
     yield request.param
     lib.pfg_set_kernel_variant(0)
+    lib.pfg_tune(5, 0)
     assert _lib.device_error() == 0, "a bounded device-side wait ran out"
 
 
