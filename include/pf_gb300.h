@@ -256,6 +256,27 @@ int pfg_batch_step(const void* device_table, int k, void* stream);
  * replay of k_steps launches), so replays need no host-side table writes. */
 int pfg_batch_advance(void* device_table, int k_steps, void* stream);
 
+/* ---- adjoint ----------------------------------------------------------------
+ * Reverse-mode derivative of the fused heat + phase-field step, hand-written
+ * (the reference differentiates with jax.grad; it has no adjoint of the coupled
+ * run).  Given the forward state of step k (eta, Tg at time t) and the
+ * adjoints of step k+1 (lam_in = dJ/d eta^{k+1}, Tb_in = dJ/d Tg^{k+1}, both
+ * ghost faces and interior of the ghosted layout), writes lam_out = dJ/d eta^k
+ * and Tb_out = dJ/d Tg^k (interior and the six ghost faces; the caller zeroes
+ * edge/corner entries once) and adds this step's contributions to grads[0]
+ * (dJ/d beam power) and grads[1] (dJ/d scan speed, with dxl_dv = d x_beam / d v
+ * at the mid-step time).  scratch: pfg_adjoint_scratch_bytes(p) bytes. */
+int64_t pfg_adjoint_scratch_bytes(const pfg_pf_params* p);
+int pfg_adjoint_step(const pfg_pf_params* p, const pfg_heat_params* h, const float* eta,
+                     const float* Tg, double t, float dt, const float* lam_in, const float* Tb_in,
+                     float* lam_out, float* Tb_out, void* scratch, int64_t scratch_bytes,
+                     double* grads, float dxl_dv, void* stream);
+/* Objective of the differentiable run: J += mean over cells of
+ * sum_i w_i eta_i^2 (float64 accumulation into *J, which the caller zeroes),
+ * and, if lam_seed is not NULL, dJ/d eta = 2 w_i eta_i / N. */
+int pfg_objective(const pfg_pf_params* p, const float* eta, const float* w, double* J,
+                  float* lam_seed, void* stream);
+
 /* ---- diagnostics ----------------------------------------------------------
  * The metrics PFSolver.inspect_sol prints (allen_cahn.py:165-180) plus the
  * float64 free energy and per-orientation mass, reduced on the device.

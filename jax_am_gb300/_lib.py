@@ -97,6 +97,11 @@ _PROTOS = {
                               ctypes.POINTER(ctypes.c_int64)]),
     "pfg_batch_step": (_I, [_P, _I, _P]),
     "pfg_batch_advance": (_I, [_P, _I, _P]),
+    "pfg_adjoint_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(PfParams)]),
+    "pfg_adjoint_step": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(HeatParams), _P, _P,
+                              ctypes.c_double, _F, _P, _P, _P, _P, _P, ctypes.c_int64, _P, _F,
+                              _P]),
+    "pfg_objective": (_I, [ctypes.POINTER(PfParams), _P, _P, _P, _P, _P]),
     "pfg_pf_diag_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(PfParams)]),
     "pfg_pf_diag": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, ctypes.c_int64, _P,
                          _P]),
