@@ -35,7 +35,7 @@ PF_KEYS = dict(T_liquidus=1623.0, gas_const=8.3, Qg=1.4e5, L0=3.5e3, kappa_g=2.7
                ad_hoc=1.0)
 METRIC = "cell_orientation_updates_per_s"
 UNIT = "cell*ori/s"
-KERNEL = "pf_zmarch_kernel<4, true, 1> (fused heat + anisotropic phase field)"
+KERNEL = "pf_tma_kernel<ANISO=true, TSRC=heat, 256> (fused heat + anisotropic phase field)"
 
 
 def gamma_args(w):
@@ -122,7 +122,7 @@ def measured_peak():
 
 def traffic_per_launch():
     """DRAM bytes per launch of the top kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "pf_zmarch_laser_track_8M.md")
+    path = os.path.join(ROOT, "profiles", "pf_tma_laser_track_8M.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -135,9 +135,11 @@ def traffic_per_launch():
 
 
 def build_case(w, device_run=True):
+    """The laser-track workload (``jax_am_gb300.workloads.laser_track_case``)
+    at the grid of ``w``."""
     from jax_am_gb300.phase_field.allen_cahn import PFSolver
     from jax_am_gb300.phase_field.utils import Field
-    from jax_am_gb300.runner import HeatPFRun, single_track
+    from jax_am_gb300.runner import single_track
     pf_args = dict(PF_KEYS, Nx=w["Nx"], Ny=w["Ny"], Nz=w["Nz"], h=w["h"],
                    num_grains=w["num_grains"], num_oris=w["num_oris"], anisotropy=w["anisotropy"],
                    T_liquidus=w["T_liquidus"])
@@ -146,6 +148,59 @@ def build_case(w, device_run=True):
     g = gamma_args(w)
     path = single_track(50e-6, 0.5 * w["Ny"] * w["h"], w["speed"], w["power"], 1.0)
     return solver, g, path, poly
+
+
+def time_serving(num_jobs=256, rate=50.0):
+    """The serving stream (256 directional-solidification jobs, Poisson
+    arrivals at 50 jobs/s, HBM budget 120 GB): continuous batching against
+    sequential plain per-job solves (``PFSolver.stepper`` per step from
+    Python, the reference driver's loop), both against the wall clock."""
+    from jax_am_gb300.serving import BatchServer, run_sequential
+    from jax_am_gb300.workloads import serving_stream
+    t0 = time.perf_counter()
+    jobs = serving_stream(num_jobs, rate)
+    setup = time.perf_counter() - t0
+    seq_jobs = [j.fresh() for j in jobs]
+    srv = BatchServer(hbm_budget=120e9, max_jobs=256, graph_steps=16)
+    for j in jobs:
+        srv.submit(j)
+    batched = srv.run(realtime=True)
+    batched_results = [j.result for j in jobs]
+    sequential = run_sequential(seq_jobs, realtime=True)
+    worst = max(float((a - b.result).abs().max().item()) for a, b in zip(batched_results, seq_jobs))
+    return {
+        "workload": f"{num_jobs} directional-solidification jobs, Poisson {rate:g} jobs/s, "
+                    "Nx,Ny~U[32,160], Nz~U[16,64], n~U[10,30], steps~U[100,2000], "
+                    "G~U[5e5,2e6] K/m, budget 120 GB",
+        "batched": {k: batched[k] for k in ("jobs_per_s", "p50_s", "p99_s", "mean_s", "wall_s")},
+        "sequential": {k: sequential[k] for k in ("jobs_per_s", "p50_s", "p99_s", "mean_s",
+                                                 "wall_s")},
+        "jobs_per_s_ratio": batched["jobs_per_s"] / sequential["jobs_per_s"],
+        "peak_hbm_gb": srv.peak_bytes / 1e9,
+        "max_abs_diff_batched_vs_sequential": worst,
+        "setup_s": setup,
+        "gpu_launches_batched": srv.launches,
+    }
+
+
+def time_adjoint():
+    """The differentiable run (128 x 128 x 64, n = 10, 500 steps, checkpoint
+    every 25): forward, then dJ/d(P, v, eta0) by the hand-written adjoint."""
+    from jax_am_gb300.workloads import differentiable_run
+    prob, P, v = differentiable_run()
+    eta0 = prob.solver.ini_cond()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J = prob.forward(P, v, eta0)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    dP, dv, de = prob.gradient()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    return {"workload": "128x128x64 cells, 300 grains, n=10, laser 200 W 0.8 m/s, 500 steps, "
+                        "checkpoint every 25",
+            "J": J, "dJ_dP": dP, "dJ_dv": dv, "dJ_deta0_norm": float(de.norm().item()),
+            "forward_s": t1 - t0, "gradient_s": t2 - t1}
 
 
 def time_cpu_baseline(w, budget_s=15.0, threads=None, sample=(100, 50, 25), steps_max=50):
@@ -206,6 +261,27 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def profile_run(args):
+    """Eager steps of the laser-track workload, one kernel launch per step:
+    ``ncu -k regex:pf_ -s <warmup> -c 1 python bench.py --profile`` captures
+    the first timed launch."""
+    import __graft_entry__
+    __graft_entry__.build()
+    from jax_am_gb300.runner import HeatPFRun
+    from jax_am_gb300 import _lib
+    solver, g, path, poly = build_case(WORKLOAD)
+    run = HeatPFRun(solver, g, path)
+    run.run(args.warmup, graph=False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run.run(args.steps, graph=False)
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": True, "ms_per_step": e0.elapsed_time(e1) / args.steps,
+                      "plan": _lib.describe_plan(solver.params)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -214,8 +290,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="eager launches only (warmup then steps), for ncu captures")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.profile:
+        profile_run(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
@@ -228,6 +311,7 @@ def main():
     import __graft_entry__
     __graft_entry__.build()
     from jax_am_gb300.runner import HeatPFRun
+    from jax_am_gb300 import _lib
 
     w = WORKLOAD
     solver, g, path, poly = build_case(w)
@@ -281,6 +365,12 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = time_cpu_baseline(w)
+    serving = None
+    if rank == 0 and not args.no_serving:
+        serving = time_serving()
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = time_adjoint()
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -294,6 +384,8 @@ def main():
                        "l2": "inputs larger than L2 (eta 640 MB per buffer)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": gpu_launches, "clocks": clocks,
+            "plan": _lib.describe_plan(solver.params),
+            "serving": serving, "adjoint": adjoint,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -129,13 +129,13 @@ typedef struct pfg_quench {
 
 /* Results of pfg_pf_diag (device memory, written by the call). */
 typedef struct pfg_diag {
-  double energy;                 /* total free energy [J], float64 accumulation */
+  double energy;                 /* total free energy [J], compensated accumulation */
   double max_T;                  /* max over cells of T */
   int64_t n_cells;
   int64_t n_ori_changed;         /* cells whose argmax orientation differs from argmax0 */
   int64_t n_liquid;              /* cells with T >= T_liquidus */
   int64_t n_nonfinite;           /* eta entries that are NaN or Inf */
-  double mass[PFG_MAX_ORIS];     /* sum over cells of eta_i, float64 accumulation */
+  double mass[PFG_MAX_ORIS];     /* sum over cells of eta_i, compensated accumulation */
 } pfg_diag;
 
 /* ---- library information ----------------------------------------------- */
@@ -249,9 +249,12 @@ int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* table, int64
 /* Launch k of a replay: every job with base_step + k < target_steps takes
  * one step from eta[(base_step + k) & 1] into the other buffer, at time
  * t0 + (base_step + k) dt.  device_table: the encoded table in device
- * memory.  The grid is fixed (persistent CTAs), so the launch can be captured
- * once and replayed while the table's contents change. */
-int pfg_batch_step(const void* device_table, int k, void* stream);
+ * memory; the launch uses a work counter in its header and leaves it at zero
+ * when it ends (launches on one table must not overlap).  The grid is fixed
+ * (persistent CTAs), so the launch can be captured once and replayed while
+ * the table's contents change.  Jobs are stored in the table by unit cost,
+ * largest first, not in the caller's order. */
+int pfg_batch_step(void* device_table, int k, void* stream);
 /* Add k_steps to every job's base_step in the device table (the end of a
  * replay of k_steps launches), so replays need no host-side table writes. */
 int pfg_batch_advance(void* device_table, int k_steps, void* stream);
@@ -279,7 +282,10 @@ int pfg_objective(const pfg_pf_params* p, const float* eta, const float* w, doub
 
 /* ---- diagnostics ----------------------------------------------------------
  * The metrics PFSolver.inspect_sol prints (allen_cahn.py:165-180) plus the
- * float64 free energy and per-orientation mass, reduced on the device.
+ * free energy and per-orientation mass, reduced on the device.  The mass is
+ * a compensated (error-free) sum returned as float64; the energy sums
+ * float32 per-cell energy densities (relative error ~1e-7 per cell) with
+ * compensated accumulation.  Fewer than 2^31 cells.
  *  T:         per-cell (nz, ny, nx) when T_ghosted == 0, else the ghosted
  *             (nz+2, ny+2, nx+2) heat state.
  *  argmax0:   (nz, ny, nx) int32 reference orientation map, or NULL (then

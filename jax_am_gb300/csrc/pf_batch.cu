@@ -11,10 +11,18 @@
 // change, a graph of K launches (k = 0 .. K-1) is captured once and replayed
 // while the host rewrites the table between replays (admitting and retiring
 // jobs: continuous batching).
+//
+// Units are handed out dynamically: each CTA takes the next unit from a
+// counter in the table header, and the encoder orders the jobs by unit cost,
+// largest first, so that units of very different sizes (jobs differ tenfold
+// in tile and column size) still finish together.  The last CTA of a launch
+// to run out of units resets the counter for the next launch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
+#include <utility>
+#include <vector>
 
 #include "pfg_host.h"
 #include "pfg_step.cuh"
@@ -34,29 +42,40 @@ struct BatchJobDev {
 struct BatchHeader {
   int num_jobs, pad;
   long long total_units;
+  unsigned long long next_unit;  // dynamic unit counter (zero between launches)
+  unsigned int done_ctas;        // CTAs of this launch that ran out of units
+  int pad2;
 };
+static_assert(sizeof(BatchHeader) % 16 == 0, "job records follow the header 16-byte aligned");
 
 constexpr int kBatchVersion = 1;
 
 __global__ void __launch_bounds__(kThreads, 2)
-pf_batch_kernel(const BatchHeader* __restrict__ hdr, int k) {
+pf_batch_kernel(BatchHeader* __restrict__ hdr, int k) {
   extern __shared__ __align__(16) float smem[];
   __shared__ __align__(16) StepArgs s_args;
   __shared__ int s_job;
+  __shared__ long long s_unit;
   const BatchJobDev* jobs = reinterpret_cast<const BatchJobDev*>(hdr + 1);
   const long long total = hdr->total_units;
   const int nj = hdr->num_jobs;
-  for (long long u = blockIdx.x; u < total; u += gridDim.x) {
+  for (;;) {
     if (threadIdx.x == 0) {
-      int lo = 0, hi = nj - 1;  // last job whose first unit is <= u
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (jobs[mid].unit_begin <= u) lo = mid;
-        else hi = mid - 1;
+      const long long u = (long long)atomicAdd(&hdr->next_unit, 1ULL);
+      s_unit = u;
+      if (u < total) {
+        int lo = 0, hi = nj - 1;  // last job whose first unit is <= u
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (jobs[mid].unit_begin <= u) lo = mid;
+          else hi = mid - 1;
+        }
+        s_job = lo;
       }
-      s_job = lo;
     }
     __syncthreads();
+    const long long u = s_unit;
+    if (u >= total) break;  // uniform across the CTA
     const BatchJobDev& J = jobs[s_job];
     const long long step = J.base_step + k;
     if (step < J.target_steps) {  // uniform over the CTA
@@ -84,6 +103,14 @@ pf_batch_kernel(const BatchHeader* __restrict__ hdr, int k) {
       }
     }
     __syncthreads();  // shared memory is reused by the next unit
+  }
+  // the last CTA out resets the counter: every CTA has stopped taking units
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&hdr->done_ctas, 1u) == gridDim.x - 1) {
+      atomicExch(&hdr->next_unit, 0ULL);
+      atomicExch(&hdr->done_ctas, 0u);
+    }
   }
 }
 
@@ -123,7 +150,8 @@ extern "C" int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* t
   const size_t budget = batch_smem_budget(d);
   BatchHeader* hdr = static_cast<BatchHeader*>(table);
   BatchJobDev* out = reinterpret_cast<BatchJobDev*>(hdr + 1);
-  long long units = 0;
+  std::vector<TilePlan> plans((size_t)num_jobs);
+  std::vector<std::pair<double, int>> order((size_t)num_jobs);
   for (int j = 0; j < num_jobs; ++j) {
     const pfg_batch_job& J = jobs[j];
     int st = check_pf_params(&J.params);
@@ -131,16 +159,33 @@ extern "C" int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* t
     if (!J.eta[0] || !J.eta[1]) return PFG_ERR_NULL;
     if (!aligned16(J.eta[0]) || !aligned16(J.eta[1])) return PFG_ERR_ALIGN;
     if (J.eta[0] == J.eta[1] || J.target_steps < 0 || J.base_step < 0) return PFG_ERR_PARAM;
-    TilePlan t;
-    if (!plan_warp_tiles_budget(J.params.nx, J.params.ny, J.params.nz, J.params.num_oris,
-                                d.sm_count, budget, &t))
+    TilePlan& t = plans[(size_t)j];
+    // tiles chosen for cover and halo only: the batch has units enough to
+    // fill the GPU whatever their count
+    if (!plan_warp_tiles_ex(J.params.nx, J.params.ny, J.params.nz, J.params.num_oris,
+                            d.sm_count, budget, kThreads / 32, 0, 1 << 30, &t))
       return PFG_ERR_SHAPE;  // orientation count the warp-per-cells body cannot take
-    // units of whole z columns (or 32-plane chunks): the batch has plenty of units
-    const int zch = std::max(1, (J.params.nz + 31) / 32);
+    // units of whole z columns (or 64-plane chunks), so that few halo planes
+    // are read twice
+    const int zch = std::max(1, (J.params.nz + 63) / 64);
     t.zc = (J.params.nz + zch - 1) / zch;
     t.zchunks = (J.params.nz + t.zc - 1) / t.zc;
     t.units = (long)t.tiles_x * t.tiles_y * t.zchunks;
-    BatchJobDev& D = out[j];
+    // bytes a unit moves: its tile with halo, its planes with halo, n floats
+    const double cost = (double)(t.tx + 2) * (t.ty + 2) * (t.zc + 2) * J.params.num_oris;
+    order[(size_t)j] = {-cost, j};
+  }
+  // largest units first (stable: equal costs keep the caller's order)
+  std::stable_sort(order.begin(), order.end(),
+                   [](const std::pair<double, int>& x, const std::pair<double, int>& y) {
+                     return x.first < y.first;
+                   });
+  long long units = 0;
+  for (int r = 0; r < num_jobs; ++r) {
+    const int j = order[(size_t)r].second;
+    const pfg_batch_job& J = jobs[j];
+    const TilePlan& t = plans[(size_t)j];
+    BatchJobDev& D = out[r];
     std::memset(&D, 0, sizeof(D));
     fill_step_args(D.args, J.params, t, J.dt);
     D.args.cpw = t.cpw; D.args.wx = t.wx; D.args.rpw = t.rpw;
@@ -159,11 +204,14 @@ extern "C" int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* t
   hdr->num_jobs = num_jobs;
   hdr->pad = kBatchVersion;
   hdr->total_units = units;
+  hdr->next_unit = 0;
+  hdr->done_ctas = 0;
+  hdr->pad2 = 0;
   if (total_units) *total_units = units;
   return PFG_OK;
 }
 
-extern "C" int pfg_batch_step(const void* device_table, int k, void* stream) {
+extern "C" int pfg_batch_step(void* device_table, int k, void* stream) {
   if (!device_table) return PFG_ERR_NULL;
   if (k < 0) return PFG_ERR_PARAM;
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
@@ -178,7 +226,7 @@ extern "C" int pfg_batch_step(const void* device_table, int k, void* stream) {
     if (dev >= 0 && dev < 64) configured[dev] = (int)smem;
   }
   pf_batch_kernel<<<2 * d.sm_count, kThreads, smem, static_cast<cudaStream_t>(stream)>>>(
-      static_cast<const BatchHeader*>(device_table), k);
+      static_cast<BatchHeader*>(device_table), k);
   return record_cuda(cudaGetLastError());
 }
 

@@ -3,12 +3,26 @@
 // The reference's only observability on this path is PFSolver.inspect_sol
 // (allen_cahn.py:165-180): percentage of cells whose argmax orientation
 // changed, percentage of cells at or above the liquidus, max T and a NaN
-// check.  This computes those counts plus the float64 free energy and
-// per-orientation mass in one pass.  One warp handles one cell at a time,
-// lanes spanning the orientations, so loads are coalesced and the argmax and
-// sums are warp shuffles.  Per-block partial records go to a caller-provided
-// scratch buffer; a second one-block kernel folds them in a fixed order, so
-// the result is bit-reproducible.
+// check.  This computes those counts plus the free energy and the
+// per-orientation mass in one pass over eta.
+//
+// Layout of the work: a group of G lanes (G a power of two, 4 G >= n) owns one
+// cell, each lane a fixed set of up to four orientations (a 16-byte vector
+// when n % 4 == 0), so a warp covers 32 / G cells per iteration with coalesced
+// loads, and each lane keeps the running mass of its own orientations in
+// registers.  Per-cell sums (sum eta^2, sum eta^4, gradient energy, argmax)
+// are FP32 butterflies over the group.
+//
+// Precision.  GB300 issues FP64 at a small fraction of its FP32 rate, so no
+// FP64 instruction runs per element or per cell: the mass and the energy are
+// accumulated per thread with compensated FP32 sums (Knuth's TwoSum: the
+// rounding error of every addition is carried in a second word), which is as
+// accurate as FP64 accumulation for these sums, and the per-thread (hi, lo)
+// pairs are folded in FP64 at the end of the block.  The per-cell local and
+// gradient energy densities are evaluated in FP32 (a few roundings, relative
+// error ~1e-7 of the cell's energy).  Per-block partial records go to a
+// caller-provided scratch buffer; a second one-block kernel folds them in a
+// fixed order, so the result is bit-reproducible.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -30,8 +44,12 @@ struct DiagArgs {
   int nx, ny, nz, n;
   int bcx, bcy, bcz;
   int T_ghosted;
-  double wx, wy, wz;  // 1/h per axis
-  double m_g, kappa_half, vol, T_liq;
+  float gwx, gwy, gwz;  // kappa_g / 2 / h_d^2: the gradient energy weight per axis
+  float m_g, vol;
+  // T_liq (double) compared with float T exactly: T >= T_liq <=> T >= tl_ge
+  // (the smallest float >= T_liq); T == T_liq <=> T == tl_eq (NaN when T_liq
+  // is not a float)
+  float tl_ge, tl_eq;
   const float* eta;
   const float* T;
   const int32_t* argmax0;
@@ -40,6 +58,7 @@ struct DiagArgs {
 };
 
 constexpr int kDiagBlocks = 296;  // 2 x 148..152 SMs; fixed so results do not depend on the GPU
+constexpr int kDiagThreads = 512;
 
 __device__ __forceinline__ bool argmax_better(float a, int ia, float b, int ib) {
   // np.argmax semantics: the first NaN wins, otherwise the first maximum
@@ -48,71 +67,121 @@ __device__ __forceinline__ bool argmax_better(float a, int ia, float b, int ib) 
   return a > b || (a == b && ia < ib);
 }
 
-__global__ void __launch_bounds__(256) pf_diag_kernel(const __grid_constant__ DiagArgs a) {
-  __shared__ double s_mass[8][PFG_MAX_ORIS];
-  __shared__ double s_energy[8], s_maxT[8];
-  __shared__ long long s_cnt[8][3];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long ncell = (long long)a.nx * a.ny * a.nz;
-  const long long gwarp = (long long)blockIdx.x * 8 + warp;
-  const long long nwarps = (long long)gridDim.x * 8;
-  const int n = a.n;
-  double mass0 = 0.0, mass1 = 0.0, energy = 0.0, maxT = -INFINITY;
-  long long changed = 0, liquid = 0, nonfinite = 0;
-  const int64_t sy = (int64_t)a.nx * n, sz = (int64_t)a.ny * a.nx * n;
-  for (long long c = gwarp; c < ncell; c += nwarps) {
-    const int x = (int)(c % a.nx);
-    const int y = (int)((c / a.nx) % a.ny);
-    const int z = (int)(c / ((long long)a.nx * a.ny));
-    const float* e = a.eta + c * n;
-    const float v0 = (lane < n) ? e[lane] : 0.f;
-    const float v1 = (lane + 32 < n) ? e[lane + 32] : 0.f;
-    if (lane < n && !isfinite(v0)) ++nonfinite;
-    if (lane + 32 < n && !isfinite(v1)) ++nonfinite;
-    mass0 += v0;
-    mass1 += v1;
-    // argmax over the cell's orientations
-    float best = (lane < n) ? v0 : -INFINITY;
-    int bi = (lane < n) ? lane : 1 << 30;
-    if (lane + 32 < n && argmax_better(v1, lane + 32, best, bi)) { best = v1; bi = lane + 32; }
+// Compensated running sum: hi + lo is the sum of everything added, to within
+// the rounding of lo (Knuth's TwoSum gives the exact error of each addition).
+struct CSum {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(s, hi);
+    const float ap = __fsub_rn(s, bp);
+    const float err = __fadd_rn(__fsub_rn(hi, ap), __fsub_rn(x, bp));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// Lane's orientation v (0..3) of its group slot g: vector layout (n % 4 == 0)
+// holds 4 g .. 4 g + 3, strided layout g, g + G, g + 2 G, g + 3 G.
+template <int G, bool VEC4>
+__device__ __forceinline__ int ori_of(int g, int v) {
+  return VEC4 ? 4 * g + v : g + G * v;
+}
+
+template <int G, bool VEC4>
+__device__ __forceinline__ void load4(const float* p, int g, int n, float (&out)[4]) {
+  if constexpr (VEC4) {
+    if (4 * g < n) {
+      const float4 u = __ldg(reinterpret_cast<const float4*>(p) + g);
+      out[0] = u.x; out[1] = u.y; out[2] = u.z; out[3] = u.w;
+    } else {
+      out[0] = out[1] = out[2] = out[3] = 0.f;
+    }
+  } else {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    for (int v = 0; v < 4; ++v) {
+      const int i = g + G * v;
+      out[v] = (i < n) ? __ldg(p + i) : 0.f;
+    }
+  }
+}
+
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// Cell iterations between a group's L2 prefetch and its load of that cell:
+// keeps several lines per warp in flight without holding them in registers.
+constexpr int kDiagPrefetch = 4;
+
+template <int G, bool VEC4>
+__global__ void __launch_bounds__(kDiagThreads)
+pf_diag_kernel(const __grid_constant__ DiagArgs a) {
+  constexpr int kWarps = kDiagThreads / 32;
+  constexpr int kCellsPerWarp = 32 / G;
+  __shared__ double s_mass[kWarps][PFG_MAX_ORIS];
+  __shared__ double s_energy[kWarps], s_maxT[kWarps];
+  __shared__ long long s_cnt[kWarps][3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane & (G - 1);          // slot within the cell's group
+  const int cw = lane / G;               // cell within the warp
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (cw * G));
+  const int n = a.n;
+  const int ncell = a.nx * a.ny * a.nz;  // host checks < 2^31
+  const int64_t sy = (int64_t)a.nx * n;
+  const int64_t sz = (int64_t)a.ny * a.nx * n;
+  const int stride = gridDim.x * kWarps * kCellsPerWarp;
+
+  CSum mass[4], energy;
+  float maxT = -INFINITY;
+  int changed = 0, liquid = 0, nonfinite = 0;
+
+  for (int c = (blockIdx.x * kWarps + warp) * kCellsPerWarp + cw; c < ncell; c += stride) {
+    const int xy = a.nx * a.ny;
+    const int z = c / xy;
+    const int r = c - z * xy;
+    const int y = r / a.nx;
+    const int x = r - y * a.nx;
+    const float* e = a.eta + (int64_t)c * n;
+    {
+      const int64_t cp = (int64_t)c + (int64_t)kDiagPrefetch * stride;
+      if (cp < ncell && 4 * g < n) prefetch_l2(a.eta + cp * n + 4 * g);
+    }
+    const int64_t dx = (x + 1 < a.nx) ? n : (a.bcx ? -(int64_t)(a.nx - 1) * n : 0);
+    const int64_t dy = (y + 1 < a.ny) ? sy : (a.bcy ? -(int64_t)(a.ny - 1) * sy : 0);
+    const int64_t dz = (z + 1 < a.nz) ? sz : (a.bcz ? -(int64_t)(a.nz - 1) * sz : 0);
+    float v[4], ex[4], ey[4], ez[4];
+    load4<G, VEC4>(e, g, n, v);
+    load4<G, VEC4>(e + dx, g, n, ex);
+    load4<G, VEC4>(e + dy, g, n, ey);
+    load4<G, VEC4>(e + dz, g, n, ez);
+    float s2 = 0.f, s4 = 0.f, g2 = 0.f, best = -INFINITY;
+    int bi = 1 << 30;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = ori_of<G, VEC4>(g, k);
+      if (i < n) {
+        if (!isfinite(v[k])) ++nonfinite;
+        mass[k].add(v[k]);
+        const float q = v[k] * v[k];
+        s2 += q;
+        s4 = fmaf(q, q, s4);
+        const float gx = ex[k] - v[k], gy = ey[k] - v[k], gz = ez[k] - v[k];
+        g2 = fmaf(a.gwx * gx, gx, fmaf(a.gwy * gy, gy, fmaf(a.gwz * gz, gz, g2)));
+        if (argmax_better(v[k], i, best, bi)) { best = v[k]; bi = i; }
+      }
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+      s2 += __shfl_xor_sync(gmask, s2, o);
+      s4 += __shfl_xor_sync(gmask, s4, o);
+      g2 += __shfl_xor_sync(gmask, g2, o);
+      const float ob = __shfl_xor_sync(gmask, best, o);
+      const int oi = __shfl_xor_sync(gmask, bi, o);
       if (argmax_better(ob, oi, best, bi)) { best = ob; bi = oi; }
     }
-    // local energy terms (allen_cahn.py:42-49) in float64
-    const double d0 = v0, d1 = v1;
-    double s2 = d0 * d0 + d1 * d1;
-    double s4 = d0 * d0 * d0 * d0 + d1 * d1 * d1 * d1;
-    // gradient energy: forward differences, zero across a Neumann face
-    double g2 = 0.0;
-    {
-      const int xn = (x + 1 < a.nx) ? x + 1 : (a.bcx ? 0 : x);
-      const int yn = (y + 1 < a.ny) ? y + 1 : (a.bcy ? 0 : y);
-      const int zn = (z + 1 < a.nz) ? z + 1 : (a.bcz ? 0 : z);
-      const float* ex = a.eta + (int64_t)z * sz + (int64_t)y * sy + (int64_t)xn * n;
-      const float* ey = a.eta + (int64_t)z * sz + (int64_t)yn * sy + (int64_t)x * n;
-      const float* ez = a.eta + (int64_t)zn * sz + (int64_t)y * sy + (int64_t)x * n;
-      if (lane < n) {
-        const double gx = ((double)ex[lane] - d0) * a.wx, gy = ((double)ey[lane] - d0) * a.wy,
-                     gz = ((double)ez[lane] - d0) * a.wz;
-        g2 += gx * gx + gy * gy + gz * gz;
-      }
-      if (lane + 32 < n) {
-        const double gx = ((double)ex[lane + 32] - d1) * a.wx,
-                     gy = ((double)ey[lane + 32] - d1) * a.wy,
-                     gz = ((double)ez[lane + 32] - d1) * a.wz;
-        g2 += gx * gx + gy * gy + gz * gz;
-      }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-      s4 += __shfl_xor_sync(0xffffffffu, s4, o);
-      g2 += __shfl_xor_sync(0xffffffffu, g2, o);
-    }
-    if (lane == 0) {
+    if (g == 0) {
       float T;
       if (a.T_ghosted) {
         const int64_t gsy = a.nx + 2, gsz = (int64_t)(a.ny + 2) * (a.nx + 2);
@@ -120,51 +189,77 @@ __global__ void __launch_bounds__(256) pf_diag_kernel(const __grid_constant__ Di
       } else {
         T = a.T[c];
       }
-      const double Tc = (T > 2000.f) ? 2000.0 : (double)T;
-      const double zeta = 0.5 * (1.0 - tanh(1e10 * (Tc / a.T_liq - 1.0)));
-      const double om = 1.0 - zeta;
-      const double f_loc = a.m_g * ((s4 / 4.0 - s2 / 2.0) + (s2 * s2 - s4) + om * om * s2);
-      energy += (f_loc + a.kappa_half * g2) * a.vol;
-      if ((double)T >= a.T_liq) ++liquid;
-      if ((double)T > maxT || isnan(T)) maxT = isnan(maxT) ? maxT : (double)T;
+      // 1 - zeta of allen_cahn.py:56-57: the tanh is +-1 unless T_c == T_liq
+      // (a float32 T differs from T_liq by at least 7e-8 relative, times 1e10)
+      const float Tc = fminf(T, 2000.f);
+      const float om = isnan(T) ? T : (Tc == a.tl_eq ? 0.5f : (Tc >= a.tl_ge ? 1.f : 0.f));
+      const float f_loc =
+          a.m_g * ((0.25f * s4 - 0.5f * s2) + fmaf(s2, s2, -s4) + om * om * s2);
+      energy.add((f_loc + g2) * a.vol);
+      if (T >= a.tl_ge) ++liquid;
+      if (T > maxT || isnan(T)) maxT = isnan(maxT) ? maxT : T;
       if (a.argmax_out) a.argmax_out[c] = bi;
       if (a.argmax0 && a.argmax0[c] != bi) ++changed;
     }
   }
-  // block reduction
+
+  // ---- block reduction (fixed order): warp butterflies, then warps in order
+  double m[4];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) nonfinite += __shfl_xor_sync(0xffffffffu, nonfinite, o);
-  if (lane < n) s_mass[warp][lane] = mass0;
-  if (lane + 32 < n) s_mass[warp][lane + 32] = mass1;
+  for (int k = 0; k < 4; ++k) m[k] = mass[k].value();
+  double en = energy.value();
+  double mt = (double)maxT;
+  long long c0 = changed, c1 = liquid, c2 = nonfinite;
+#pragma unroll
+  for (int o = 16; o >= G; o >>= 1) {  // lanes with the same slot hold the same orientations
+#pragma unroll
+    for (int k = 0; k < 4; ++k) m[k] += __shfl_xor_sync(0xffffffffu, m[k], o);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    en += __shfl_xor_sync(0xffffffffu, en, o);
+    const double om = __shfl_xor_sync(0xffffffffu, mt, o);
+    if (om > mt || isnan(om)) mt = isnan(mt) ? mt : om;
+    c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+    c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+    c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+  }
+  if (lane < G) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = ori_of<G, VEC4>(lane, k);
+      if (i < n) s_mass[warp][i] = m[k];
+    }
+  }
   if (lane == 0) {
-    s_energy[warp] = energy;
-    s_maxT[warp] = maxT;
-    s_cnt[warp][0] = changed;
-    s_cnt[warp][1] = liquid;
-    s_cnt[warp][2] = nonfinite;
+    s_energy[warp] = en;
+    s_maxT[warp] = mt;
+    s_cnt[warp][0] = c0;
+    s_cnt[warp][1] = c1;
+    s_cnt[warp][2] = c2;
   }
   __syncthreads();
   DiagPartial* out = a.partials + blockIdx.x;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    double m = 0.0;
-    for (int w = 0; w < 8; ++w) m += s_mass[w][i];
-    out->mass[i] = m;
+    double s = 0.0;
+    for (int w = 0; w < kWarps; ++w) s += s_mass[w][i];
+    out->mass[i] = s;
   }
   if (threadIdx.x == 0) {
-    double en = 0.0, mt = -INFINITY;
-    long long c0 = 0, c1 = 0, c2 = 0;
-    for (int w = 0; w < 8; ++w) {
-      en += s_energy[w];
-      if (s_maxT[w] > mt || isnan(s_maxT[w])) mt = isnan(mt) ? mt : s_maxT[w];
-      c0 += s_cnt[w][0];
-      c1 += s_cnt[w][1];
-      c2 += s_cnt[w][2];
+    double e2 = 0.0, t2 = -INFINITY;
+    long long d0 = 0, d1 = 0, d2 = 0;
+    for (int w = 0; w < kWarps; ++w) {
+      e2 += s_energy[w];
+      if (s_maxT[w] > t2 || isnan(s_maxT[w])) t2 = isnan(t2) ? t2 : s_maxT[w];
+      d0 += s_cnt[w][0];
+      d1 += s_cnt[w][1];
+      d2 += s_cnt[w][2];
     }
-    out->energy = en;
-    out->max_T = mt;
-    out->changed = c0;
-    out->liquid = c1;
-    out->nonfinite = c2;
+    out->energy = e2;
+    out->max_T = t2;
+    out->changed = d0;
+    out->liquid = d1;
+    out->nonfinite = d2;
   }
 }
 
@@ -196,28 +291,57 @@ pf_diag_finish_kernel(const DiagPartial* __restrict__ parts, int nparts, int n, 
   }
 }
 
+// lanes per cell: the smallest power of two G with 4 G >= n (n <= 64)
+static int diag_group(int n) {
+  int g = 1;
+  while (4 * g < n) g *= 2;
+  return g;
+}
+
 int diag_blocks(const pfg_pf_params& p) {
   const long long ncell = (long long)p.nx * p.ny * p.nz;
-  const long long need = (ncell + 7) / 8;
+  const long long per_block = (kDiagThreads / 32) * (32 / diag_group(p.num_oris));
+  const long long need = (ncell + per_block - 1) / per_block;
   return (int)(need < kDiagBlocks ? need : kDiagBlocks);
+}
+
+template <int G>
+static void launch_diag_g(const DiagArgs& a, int nb, cudaStream_t s) {
+  if (a.n % 4 == 0) pf_diag_kernel<G, true><<<nb, kDiagThreads, 0, s>>>(a);
+  else pf_diag_kernel<G, false><<<nb, kDiagThreads, 0, s>>>(a);
 }
 
 int launch_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_ghosted,
                 const int32_t* argmax0, int32_t* argmax_out, void* scratch,
                 pfg_diag* out, cudaStream_t s) {
+  // cell indices are 32-bit in the reduction
+  if ((int64_t)p->nx * p->ny * p->nz >= ((int64_t)1 << 31)) return PFG_ERR_SHAPE;
   DiagArgs a{};
   a.nx = p->nx; a.ny = p->ny; a.nz = p->nz; a.n = p->num_oris;
   a.bcx = p->bc_x; a.bcy = p->bc_y; a.bcz = p->bc_z;
   a.T_ghosted = T_ghosted;
-  a.wx = 1.0 / p->h_x; a.wy = 1.0 / p->h_y; a.wz = 1.0 / p->h_z;
-  a.m_g = p->m_g;
-  a.kappa_half = 0.5 * (double)p->kappa_g;
-  a.vol = (double)p->h_x * p->h_y * p->h_z;
-  a.T_liq = p->T_liquidus;
+  a.gwx = (float)(0.5 * (double)p->kappa_g / ((double)p->h_x * p->h_x));
+  a.gwy = (float)(0.5 * (double)p->kappa_g / ((double)p->h_y * p->h_y));
+  a.gwz = (float)(0.5 * (double)p->kappa_g / ((double)p->h_z * p->h_z));
+  a.m_g = (float)p->m_g;
+  a.vol = (float)((double)p->h_x * p->h_y * p->h_z);
+  {
+    const double tl = p->T_liquidus;
+    float f = (float)tl;
+    if ((double)f < tl) f = nextafterf(f, INFINITY);
+    a.tl_ge = f;
+    a.tl_eq = ((double)(float)tl == tl) ? (float)tl : NAN;
+  }
   a.eta = eta; a.T = T; a.argmax0 = argmax0; a.argmax_out = argmax_out;
   a.partials = static_cast<DiagPartial*>(scratch);
   const int nb = diag_blocks(*p);
-  pf_diag_kernel<<<nb, 256, 0, s>>>(a);
+  switch (diag_group(a.n)) {
+    case 1: launch_diag_g<1>(a, nb, s); break;
+    case 2: launch_diag_g<2>(a, nb, s); break;
+    case 4: launch_diag_g<4>(a, nb, s); break;
+    case 8: launch_diag_g<8>(a, nb, s); break;
+    default: launch_diag_g<16>(a, nb, s); break;
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return record_cuda(e);
   pf_diag_finish_kernel<<<1, 256, 0, s>>>(a.partials, nb, p->num_oris,

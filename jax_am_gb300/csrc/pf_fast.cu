@@ -77,7 +77,9 @@ bool plan_warp_tiles_budget(int nx, int ny, int nz, int n, int sm_count, size_t 
 }
 
 // warps: warps that own cells (the tile is wx * cpw by (warps / wx) * rpw cells);
-// ctas_per_sm: for the wave count; max_cells: cap on tile cells.
+// ctas_per_sm: for the wave count (0: the units share the GPU with other work,
+// as in the batched step, so waves are not counted); max_cells: cap on tile
+// cells.
 bool plan_warp_tiles_ex(int nx, int ny, int nz, int n, int sm_count, size_t budget, int warps,
                         int ctas_per_sm, int max_cells, TilePlan* out) {
   TilePlan t{};
@@ -110,7 +112,7 @@ bool plan_warp_tiles_ex(int nx, int ny, int nz, int n, int sm_count, size_t budg
       zch = std::max(1L, std::min(zch, (long)std::max(1, nz / 8)));
       const long zc = (nz + zch - 1) / zch;
       const double waves = (double)(tiles * ((nz + zc - 1) / zc)) / (double)concurrent;
-      const double wave_eff = waves / std::ceil(waves);
+      const double wave_eff = concurrent > 0 ? waves / std::ceil(waves) : 1.0;
       // measured on GB300: halo columns cost about twice what halo rows cost
       // (every staged row carries its two x-halo cells)
       const double hx = (double)(tx + 2) / tx, hy = (double)(ty + 2) / ty;

@@ -240,14 +240,25 @@ class PFSolver:
         }
 
     def stable_dt(self, T_max=2000.0, safety=0.9):
-        """Largest stable explicit dt at temperatures up to ``T_max``: the
-        diffusive limit h^2 / (2 sum 1/h_d^2 Lg kappa_g ad_hoc (1 + A)) with
-        Lg = L0 exp(-Qg / (R min(T_max, 2000)))."""
-        a = self.pf_args
+        """Largest stable explicit dt at temperatures up to ``T_max`` (see
+        ``stable_dt_for``) for this solver's grid."""
+        p = self.params
+        return PFSolver.stable_dt_for(self.pf_args, T_max, safety, (p.h_x, p.h_y, p.h_z))
+
+    @staticmethod
+    def stable_dt_for(pf_args, T_max=2000.0, safety=0.9, h=None):
+        """The diffusive limit 1 / (2 sum_d 1/h_d^2 Lg kappa_g ad_hoc (1 + A))
+        with Lg = L0 exp(-Qg / (R min(T_max, 2000))), times ``safety``.
+        ``h`` defaults to ``pf_args['h']`` or domain / N."""
+        a = pf_args
+        if h is None:
+            if "h" in a:
+                h = (a["h"],) * 3 if np.isscalar(a["h"]) else tuple(a["h"])
+            else:
+                h = (a["domain_x"] / a["Nx"], a["domain_y"] / a["Ny"], a["domain_z"] / a["Nz"])
         T = min(float(T_max), 2000.0)
         Lg = a["L0"] * np.exp(-a["Qg"] / (a["gas_const"] * T))
-        p = self.params
-        s = 1.0 / p.h_x ** 2 + 1.0 / p.h_y ** 2 + 1.0 / p.h_z ** 2
+        s = sum(1.0 / float(v) ** 2 for v in h)
         lim = 1.0 / (2.0 * s * Lg * a["kappa_g"] * a["ad_hoc"] * (1.0 + a["anisotropy"]))
         return safety * lim
 

@@ -53,8 +53,9 @@ class Job:
     finished: float = float("nan")
     result: Optional[torch.Tensor] = None
     _params: object = field(default=None, repr=False)
-    _eta: Optional[torch.Tensor] = field(default=None, repr=False)
+    _eta: Optional[list] = field(default=None, repr=False)  # the two eta buffers
     _base: int = 0
+    _n_store: int = 0  # orientations per cell as stored on the device (padded)
 
     @property
     def cells(self):
@@ -67,11 +68,28 @@ class Job:
     @property
     def nbytes(self):
         """HBM held while active: the float32 eta double buffer."""
-        return 2 * self.cells * self.num_oris * 4
+        return 2 * self.cells * (self._n_store or self.num_oris) * 4
 
     @property
     def latency(self):
         return self.finished - self.arrival
+
+    def fresh(self):
+        """The same job (inputs shared) with no run state."""
+        return Job(self.pf_args, self.polycrystal, self.quench, self.steps, self.dt,
+                   arrival=self.arrival, eta0=self.eta0, t0=self.t0)
+
+
+class _PaddedDirections:
+    """A polycrystal view whose orientation list is padded with zero
+    directions to ``n_store`` entries."""
+
+    def __init__(self, polycrystal, n_store):
+        self.mesh_h_xyz = polycrystal.mesh_h_xyz
+        d = np.asarray(polycrystal.unique_grain_directions, dtype=np.float64)
+        pad = np.zeros((3, n_store, 3))
+        pad[:, : d.shape[1]] = d
+        self.unique_grain_directions = pad
 
 
 def one_hot(polycrystal, N, n):
@@ -84,8 +102,13 @@ def one_hot(polycrystal, N, n):
 class BatchServer:
     """Continuously batched solver for many independent jobs on one GPU."""
 
-    def __init__(self, hbm_budget=120e9, max_jobs=256, graph_steps=16):
+    def __init__(self, hbm_budget=120e9, max_jobs=256, graph_steps=16, pad_oris=True):
         self.lib = _lib.load()
+        # Store every job with its orientation count rounded up to a multiple
+        # of 4 (extra orientations are zero and stay exactly zero: their
+        # Laplacian and bulk terms vanish), so that every cell is a whole
+        # number of 16-byte vectors and the batch kernel's vector path runs.
+        self.pad_oris = bool(pad_oris)
         self.hbm_budget = float(hbm_budget)
         self.max_jobs = int(max_jobs)
         self.graph_steps = int(graph_steps)
@@ -105,11 +128,20 @@ class BatchServer:
 
     # ---- submission and admission -------------------------------------------
     def submit(self, job: Job):
+        n = job.num_oris
+        n_store = 4 * ((n + 3) // 4) if self.pad_oris else n
+        if n_store > _lib.MAX_ORIS:
+            n_store = n
+        job._n_store = n_store
         if job.nbytes > self.hbm_budget:
             raise ValueError(f"job needs {job.nbytes} bytes, more than the HBM budget")
         job.id = self._next_id
         self._next_id += 1
-        job._params = make_pf_params(job.pf_args, job.polycrystal)
+        if n_store == n:
+            job._params = make_pf_params(job.pf_args, job.polycrystal)
+        else:
+            job._params = make_pf_params(dict(job.pf_args, num_oris=n_store),
+                                         _PaddedDirections(job.polycrystal, n_store))
         self.queue.append(job)
         return job.id
 
@@ -118,10 +150,17 @@ class BatchServer:
         while (self.queue and self.queue[0].arrival <= now and len(self.active) < self.max_jobs
                and self.used_bytes + self.queue[0].nbytes <= self.hbm_budget):
             job = self.queue.pop(0)
-            N, n = job.cells, job.num_oris
-            job._eta = torch.empty((2, N, n), dtype=torch.float32, device="cuda")
+            N, n, ns = job.cells, job.num_oris, job._n_store
+            # two allocations: a (2, N, n) tensor would put the second buffer
+            # at N*n*4 bytes, not 16-byte aligned for odd N*n
+            job._eta = [torch.empty((N, ns), dtype=torch.float32, device="cuda") for _ in range(2)]
             src = job.eta0 if job.eta0 is not None else one_hot(job.polycrystal, N, n)
-            job._eta[0].copy_(src.reshape(N, n))
+            src = torch.as_tensor(src, dtype=torch.float32, device="cuda").reshape(N, n)
+            if ns == n:
+                job._eta[0].copy_(src)
+            else:
+                job._eta[0].zero_()
+                job._eta[0][:, :n].copy_(src)
             job._base = 0
             job.admitted = now
             self.used_bytes += job.nbytes
@@ -212,7 +251,8 @@ class BatchServer:
                 self._inflight.clear()
                 for job in finished:
                     job.finished = t_done
-                    job.result = job._eta[job.steps & 1].clone()
+                    job.result = job._eta[job.steps & 1][:, : job.num_oris].clone(
+                        memory_format=torch.contiguous_format)
                     job._eta = None
                     self.active.remove(job)
                     self.used_bytes -= job.nbytes

@@ -1,5 +1,7 @@
-"""The on-device diagnostics (PFSolver.inspect_sol's metrics, float64 energy
-and mass, argmax map) against the oracle."""
+"""The on-device diagnostics (PFSolver.inspect_sol's metrics, energy and
+mass, argmax map) against the oracle.  Tolerances: counts, max T and the
+argmax map exact; mass 1e-12 relative (compensated sums); energy 1e-6
+relative (float32 per-cell energy densities, compensated accumulation)."""
 import numpy as np
 import pytest
 import torch
@@ -8,6 +10,7 @@ from oracle import pf_oracle as O
 from tests.cases import f32, pf_case
 
 pytestmark = pytest.mark.gpu
+ENERGY_RTOL = 1e-6
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -17,7 +20,9 @@ def _built():
 
 
 @pytest.mark.parametrize("shape,n,bc", [((9, 7, 5), 5, None), ((17, 13, 6), 20, "periodic"),
-                                        ((4, 4, 4), 33, None), ((31, 2, 3), 64, None)])
+                                        ((4, 4, 4), 33, None), ((31, 2, 3), 64, None),
+                                        ((64, 48, 40), 20, None), ((50, 40, 30), 7, "periodic"),
+                                        ((2, 1, 1), 1, None), ((3, 1, 2), 12, None)])
 def test_diag_vs_oracle(shape, n, bc):
     from jax_am_gb300.phase_field.allen_cahn import PFSolver
     poly, eta, T, pf_args, oargs, obc = pf_case(shape, n, 0.0, seed=12, bc=bc)
@@ -35,7 +40,7 @@ def test_diag_vs_oracle(shape, n, bc):
     assert d["n_nonfinite"] == 0
     np.testing.assert_allclose(d["mass"], eta.sum(axis=0), rtol=1e-12)
     e_ref = O.free_energy(eta, T, oargs, None, obc)
-    assert d["energy"] == pytest.approx(e_ref, rel=1e-9)
+    assert d["energy"] == pytest.approx(e_ref, rel=ENERGY_RTOL)
     am = s.argmax(torch.tensor(eta, dtype=torch.float32, device="cuda")).cpu().numpy()
     np.testing.assert_array_equal(am, np.argmax(eta.astype(np.float32), axis=1))
 

@@ -34,7 +34,8 @@ def make_job(shape, n, steps, seed, grad=1e6, arrival=0.0, aniso=0.0):
 
 def _mix():
     return [make_job((40, 33, 17), 10, 37, 1), make_job((24, 31, 9), 12, 50, 2, aniso=0.15),
-            make_job((17, 16, 21), 7, 23, 3), make_job((33, 9, 16), 20, 41, 4, grad=5e5)]
+            make_job((17, 16, 21), 7, 23, 3), make_job((33, 9, 16), 20, 41, 4, grad=5e5),
+            make_job((13, 11, 5), 3, 29, 5)]  # N*n odd: buffer sizes not a multiple of 16 B
 
 
 def test_batch_matches_plain_solver_and_mix_equals_alone():
