@@ -25,6 +25,7 @@
 
 #include "pfg_host.h"
 #include "pfg_step.cuh"
+#include "pfg_warp.cuh"
 
 namespace pfg {
 
@@ -78,7 +79,11 @@ __device__ __forceinline__ void tma_row(void* dst, const void* src, unsigned byt
       : "memory");
 }
 
-// Folded update of one element (see pf_fast.cu for the derivation).
+// Folded update of one element (see pfg_warp.cuh for the derivation).  The
+// per-cell coefficients are k = (A1, B1, C1, W) with W = -C2 = 2 A cl w_x, and
+// the anisotropy enters through cn = -min(cos^2, 1) = max(m * rcp(-ee), -1):
+// C1 + C2 c2 (1 - c2) = C1 + W (cn + cn^2).  |e| = 0 gives m * rcp(-0) = NaN,
+// fmaxf(NaN, -1) = -1 and cn + cn^2 = 0, the reference's NaN-to-zero rule.
 struct LapConstsT {
   float ry, rz, nm;
 };
@@ -97,8 +102,8 @@ __device__ __forceinline__ float tma_update_elem(const LapConstsT& L, float e, f
     const float q2 = ee - q0 - q1;
     float m;
     asm("max.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(q0), "f"(q1), "f"(q2));
-    const float c2 = fminf(m * rcp_approx(ee), 1.f);
-    u = fmaf(k.w, fmaf(-c2, c2, c2), k.z);
+    const float cn = fmaxf(m * rcp_approx(-ee), -1.f);
+    u = fmaf(k.w, fmaf(cn, cn, cn), k.z);
   }
   return fmaf(u, lap, e * fmaf(k.y, e * e, k.x));
 }
@@ -107,7 +112,7 @@ __device__ __forceinline__ float4 tma_fold(const PFConsts& c, const TempCoef& tc
   if (tc.liquid != 0.f) return make_float4(0.f, 0.f, 0.f, 0.f);
   const float K = 4.f * S + tc.om2 - 1.f;
   const float clw = tc.cl * c.wx;
-  return make_float4(1.f + tc.cg * K, -3.f * tc.cg, clw * (1.f + c.aniso), -2.f * c.aniso * clw);
+  return make_float4(1.f + tc.cg * K, -3.f * tc.cg, clw * (1.f + c.aniso), 2.f * c.aniso * clw);
 }
 
 // NC threads (256: two CTAs per SM, or 512: one CTA per SM with a tile
@@ -116,6 +121,7 @@ template <bool ANISO, int TSRC, int NC>
 __global__ void __launch_bounds__(NC, NC == 256 ? 2 : 1)
 pf_tma_kernel(const __grid_constant__ StepArgs a) {
   constexpr int VEC = 4;
+  constexpr int kTQ = 3;  // temperature cells staged per thread and plane, at most
   extern __shared__ __align__(128) float smem[];
   const int S = a.stages;
   const int slot_floats = (a.ty + 2) * a.pitch;
@@ -139,24 +145,31 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   __shared__ int s_abort;  // set by any thread whose wait ran out; read after a barrier
+  __shared__ double s_t0;
+  __shared__ float s_beam[3];
   if (threadIdx.x == 0) {
     s_abort = 0;
     // expect-tx arrival of warp 0's lane 0 + one cp.async arrival per thread
     for (int s = 0; s < S; ++s) mbar_init(&full[s], 1 + NC);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  __syncthreads();
-
-  double t0 = 0.0;
-  if constexpr (TSRC != kTArray) {
-    t0 = a.clk_in->t;
-    if (blockIdx.x == 0 && threadIdx.x == 0 && a.clk_out) {
-      a.clk_out->t = t0 + (double)a.dt;
-      a.clk_out->step = a.clk_in->step + 1;
+    double t = 0.0;
+    if constexpr (TSRC != kTArray) {
+      t = a.clk_in->t;
+      if (blockIdx.x == 0 && a.clk_out) {
+        a.clk_out->t = t + (double)a.dt;
+        a.clk_out->step = a.clk_in->step + 1;
+      }
+    }
+    s_t0 = t;
+    if constexpr (TSRC == kTHeat) {
+      // beam position and power at mid-step, once per CTA
+      laser_at(a.hp, t + 0.5 * (double)a.dt, &s_beam[0], &s_beam[1], &s_beam[2]);
     }
   }
+  __syncthreads();
+  const double t0 = s_t0;
 
-  // ---- staging: plane j (grid plane zb - 1 + j) into slot j % S
+  // ---- staging: plane j (grid plane zb - 1 + j) into ring slot s
   const int cx0 = max(x0 - 1, 0), cx1 = min(xe + 1, a.nx);
   const int dst_cell0 = cx0 - (x0 - 1);
   const bool wrap_left = (x0 == 0) && a.bcx == PFG_BC_PERIODIC;
@@ -167,9 +180,28 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   const unsigned plane_bytes =
       (unsigned)rows * (row_bytes + (wrap_left ? cell_bytes : 0u) + (wrap_right ? cell_bytes : 0u));
   const int tp = a.tx + 2;
-  const int tcols = txv + 2;
-  auto stage = [&](int j) {
-    const int s = j % S;
+  const int gsy = a.nx + 2, gsz = (a.ny + 2) * (a.nx + 2);  // ghosted strides (host checks < 2^31)
+  // this thread's temperature cells of a plane: offsets fixed for the unit
+  int t_src[kTQ], t_dst[kTQ];
+  {
+    const int tcols = (TSRC == kTHeat) ? txv + 2 : txv;
+    const int tcount = (TSRC == kTHeat) ? rows * tcols : tyv * txv;
+    const uint64_t mg = div_magic(tcols);
+#pragma unroll
+    for (int q = 0; q < kTQ; ++q) {
+      const int i = threadIdx.x + q * NC;
+      const int r = fast_div(i, mg), c = i - r * tcols;
+      const bool ok = (TSRC != kTQuench) && i < tcount;
+      if constexpr (TSRC == kTHeat) {
+        t_src[q] = ok ? (y0 + r) * gsy + x0 + c : -1;
+        t_dst[q] = r * tp + c;
+      } else {
+        t_src[q] = ok ? (y0 + r) * a.nx + x0 + c : -1;
+        t_dst[q] = (r + 1) * tp + c + 1;
+      }
+    }
+  }
+  auto stage = [&](int j, int s) {
     const int pz = zb - 1 + j;
     if (warp == 0) {
       const int gz = bc_index(pz, a.nz, a.bcz);
@@ -187,17 +219,16 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     }
     float* ts = T_s + (size_t)s * a.tslot;
     if constexpr (TSRC == kTHeat) {
-      const int64_t gsy = a.nx + 2, gsz = (int64_t)(a.ny + 2) * (a.nx + 2);
-      for (int i = threadIdx.x; i < rows * tcols; i += NC) {
-        const int r = i / tcols, c = i - r * tcols;
-        cp_async<4>(ts + r * tp + c, a.T + (int64_t)(pz + 1) * gsz + (int64_t)(y0 + r) * gsy + x0 + c);
-      }
+      const float* tplane = a.T + (int64_t)(pz + 1) * gsz;
+#pragma unroll
+      for (int q = 0; q < kTQ; ++q)
+        if (t_src[q] >= 0) cp_async<4>(ts + t_dst[q], tplane + t_src[q]);
     } else if constexpr (TSRC == kTArray) {
       if (pz >= 0 && pz < a.nz) {
-        for (int i = threadIdx.x; i < tyv * txv; i += NC) {
-          const int r = i / txv, c = i - r * txv;
-          cp_async<4>(ts + (r + 1) * tp + c + 1, a.T + ((int64_t)pz * a.ny + y0 + r) * a.nx + x0 + c);
-        }
+        const float* tplane = a.T + (int64_t)pz * a.ny * a.nx;
+#pragma unroll
+        for (int q = 0; q < kTQ; ++q)
+          if (t_src[q] >= 0) cp_async<4>(ts + t_dst[q], tplane + t_src[q]);
       }
     }
     cp_async_mbar_arrive_noinc(&full[s]);
@@ -230,11 +261,14 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   L.nm = -2.f * (1.f + L.ry + L.rz);
 
   float xl = 0.f, yl = 0.f, Pw = 0.f;
-  if constexpr (TSRC == kTHeat) laser_at(a.hp, t0 + 0.5 * (double)a.dt, &xl, &yl, &Pw);
+  if constexpr (TSRC == kTHeat) {
+    xl = s_beam[0];
+    yl = s_beam[1];
+    Pw = s_beam[2];
+  }
 
   // ---- this thread's cells for the per-cell work (at most two), fixed per unit
   const int ncell = tyv * txv;
-  const int gsy = a.nx + 2, gsz = (a.ny + 2) * (a.nx + 2);  // ghosted strides (host checks < 2^31)
   int c_eoff[2], c_toff[2], c_cc[2], c_g[2], c_hx[2], c_hy[2];
   bool c_ok[2];
 #pragma unroll
@@ -284,12 +318,12 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     }
   };
 
-  // ---- prologue: planes 0 .. S-2 in flight, wait for planes 0, 1, 2
+  // ---- prologue: planes 0 .. S-2 in flight (slot j), wait for planes 0, 1, 2
   int issued = 0;
-  for (int j = 0; j < S - 1 && j < nplanes; ++j) { stage(j); issued = j + 1; }
+  for (int j = 0; j < S - 1 && j < nplanes; ++j) { stage(j, j); issued = j + 1; }
   bool ok = true;
-  for (int j = 0; j < 3 && ok; ++j) ok = mbar_wait(&full[j % S], (unsigned)((j / S) & 1));
-  if (ok) cell_coefs(1 % S, 0, zb);
+  for (int j = 0; j < 3 && ok; ++j) ok = mbar_wait(&full[j], 0u);  // S >= 4: first phase
+  if (ok) cell_coefs(1, 0, zb);
   else s_abort = 1;
 
   const int64_t plane_elems = (int64_t)a.ny * a.nx * n;
@@ -297,16 +331,21 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   const int64_t col_base = ((int64_t)y0 * a.nx + gx) * n + i0;
   const int r_begin = wyi * a.rpw;
   const int r_end = min(r_begin + a.rpw, tyv);
+  // ring slots of planes m, m+1, m+2 and the phase parity of plane m+2,
+  // rotated each iteration (plane j is in slot j % S)
+  int s_prev = 0, s_cur = 1, s_next = 2;
+  unsigned ph_next = 0;
   for (int z = zb; z < ze; ++z) {
     const int m = z - zb;
-    const int j_next = m + 2;
-    if (ok) ok = mbar_wait(&full[j_next % S], (unsigned)((j_next / S) & 1));
+    if (ok) ok = mbar_wait(&full[s_next], ph_next);
     if (!ok) *(volatile int*)&s_abort = 1;
     __syncthreads();  // cc[m & 1] complete; everyone finished iteration m-1
     if (*(volatile int*)&s_abort) break;  // uniform across the CTA
     // the slot of plane m-1 is free: fill it with plane m+S-1
-    if (m + S - 1 < nplanes) { stage(m + S - 1); issued = m + S; }
-    const int s_prev = m % S, s_cur = (m + 1) % S, s_next = j_next % S;
+    if (m + S - 1 < nplanes) {
+      stage(m + S - 1, s_prev == 0 ? S - 1 : s_prev - 1);
+      issued = m + S;
+    }
 
     if constexpr (TSRC == kTHeat) {
       const float* tp_ = T_s + (size_t)s_prev * a.tslot;
@@ -375,6 +414,11 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
       zp.load(e_next + off);
       row_out(r, out_row, c, xm, xp, ym, yp, zm, zp);
     }
+    // rotate the ring slots
+    s_prev = s_cur;
+    s_cur = s_next;
+    s_next = (s_next + 1 == S) ? 0 : s_next + 1;
+    if (s_next == 0) ph_next ^= 1u;
   }
   // drain: copies still in flight must land before the CTA's shared memory is
   // released (in a normal run every issued plane has been waited for already)
@@ -402,6 +446,8 @@ bool plan_tma_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_pe
   const size_t budget = (size_t)max_smem_per_sm / ctas - 2048 - 6 * sizeof(uint64_t) - 64;
   if (!plan_warp_tiles_ex(nx, ny, nz, n, sm_count, budget, warps, ctas, 2 * g_tma_consumers, &t))
     return false;
+  // each thread stages at most three temperature cells of a plane
+  if ((t.tx + 2) * (t.ty + 2) > 3 * g_tma_consumers) return false;
   // the ring's barriers sit after the coefficient buffer
   t.smem += (size_t)t.stages * sizeof(uint64_t);
   t.rs = g_tma_consumers;  // threads of this plan
