@@ -59,6 +59,19 @@ def dist_env():
     return rank, world, local
 
 
+def reduce_over_ranks(ms, units):
+    """Replicas: the slowest rank's timed region (max) and the units all
+    ranks processed (sum), over the default process group (NCCL on GPUs,
+    gloo on CPU)."""
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -341,12 +354,11 @@ def main():
     clocks = sampler.stop()
     ms = ev0.elapsed_time(ev1)
     gpu_launches = run.launches - launches0
+    units = N * n * args.steps
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms, units = reduce_over_ranks(ms, units)
     ms_per_step = ms / args.steps
-    value = N * n * args.steps * world / (ms / 1e3)
+    value = units / (ms / 1e3)
 
     # roofline of the fused kernel: one launch per step
     bytes_step = algorithmic_bytes_per_step(w)

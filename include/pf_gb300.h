@@ -16,7 +16,8 @@
  *  - The heat state Tg is float32 (nz+2, ny+2, nx+2) with one ghost layer,
  *    x fastest.  The reference holds the same ghosted field as
  *    (nx+2, ny+2, nz+2), x slowest (applications/cfd/gamma/example.py:85);
- *    the Python layer transposes at the boundary.  Ghost faces are part of
+ *    pfg_heat_step also accepts that order (pfg_heat_params.layout), so no
+ *    transpose is needed at the boundary.  Ghost faces are part of
  *    the state: each step reads the previous ghosts and writes new ones
  *    (gamma.py:23-42).  Edge and corner ghosts are never read or written.
  *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy

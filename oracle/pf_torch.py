@@ -1,4 +1,4 @@
-"""PyTorch (CPU) restatement of the fused heat + phase-field step.
+"""PyTorch restatement of the fused heat + phase-field step (any device).
 
 TEST INFRASTRUCTURE ONLY, like ``pf_oracle.py``: used by the tests (float64
 autograd as the stand-in for the reference's ``jax.grad``) and by the CPU
@@ -22,10 +22,11 @@ def _shift(e, axis, step, periodic):
     if periodic:
         return torch.roll(e, -step, dims=axis)
     n = e.shape[axis]
+    dev = e.device
     if step > 0:
-        idx = torch.cat((torch.arange(1, n), torch.tensor([n - 1])))
+        idx = torch.cat((torch.arange(1, n, device=dev), torch.tensor([n - 1], device=dev)))
     else:
-        idx = torch.cat((torch.tensor([0]), torch.arange(n - 1)))
+        idx = torch.cat((torch.tensor([0], device=dev), torch.arange(n - 1, device=dev)))
     return torch.index_select(e, axis, idx)
 
 
@@ -75,8 +76,8 @@ def heat_step(Tg, xl, yl, P, dt, g, h):
 
     I = slice(1, -1)
     T = Tg.clone()
-    x = dx / 2.0 + dx * torch.arange(nx, dtype=Tg.dtype)
-    y = dy / 2.0 + dy * torch.arange(ny, dtype=Tg.dtype)
+    x = dx / 2.0 + dx * torch.arange(nx, dtype=Tg.dtype, device=Tg.device)
+    y = dy / 2.0 + dy * torch.arange(ny, dtype=Tg.dtype, device=Tg.device)
     beam = (2.0 * P * g["eta"] / math.pi / g["r"] ** 2
             * torch.exp(-2.0 * ((x[None, :] - xl) ** 2 + (y[:, None] - yl) ** 2) / g["r"] ** 2))
     T[I, I, 0] = Tg[I, I, 1] - robin((Tg[I, I, 1] + Tg[I, I, 0]) / 2) / k[I, I, 1] * dx

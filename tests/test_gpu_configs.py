@@ -1,0 +1,147 @@
+"""The float32 GPU path against a float64 run of the oracle's PyTorch
+restatement (on the GPU, in float64) for the benchmark configurations:
+directional solidification at full size (64 x 64 x 32, n = 20, 200 steps),
+the single-track laser scan and the multi-track scan on reduced grids with
+the configurations' physics.  The error after the run is printed per
+configuration; tolerances: max |d eta| <= 1e-4, max |dT| <= 1e-3 K; argmax
+orientation maps compared exactly, and every mismatched cell must be a near
+tie in the float64 run (top-two gap within twice the eta error)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import pf_torch as PT
+
+pytestmark = pytest.mark.gpu
+ETA_TOL = 1e-4
+T_TOL = 1e-3
+PF_KEYS = dict(gas_const=8.3, Qg=1.4e5, L0=3.5e3, kappa_g=2.77e-6, m_g=2.4e5, ad_hoc=1.0)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from jax_am_gb300 import _build
+    _build.build()
+
+
+def _oracle_args(pf_args, poly):
+    a = {k: pf_args[k] for k in ("T_liquidus", "gas_const", "Qg", "L0", "kappa_g", "m_g",
+                                  "anisotropy", "ad_hoc")}
+    a["h"] = tuple(float(v) for v in poly.mesh_h_xyz)
+    return a
+
+
+def _dirs(poly):
+    d = np.asarray(poly.unique_grain_directions, dtype=np.float32).astype(np.float64)
+    return torch.tensor(d, device="cuda")
+
+
+def _compare(name, e_gpu, e_ref, T_gpu=None, T_ref=None):
+    n = e_ref.shape[-1]
+    e_ref = e_ref.reshape(-1, n)
+    e_gpu = e_gpu.double().reshape(-1, n)
+    err = float((e_gpu - e_ref).abs().max())
+    am_g = torch.argmax(e_gpu, dim=1)
+    am_r = torch.argmax(e_ref, dim=1)
+    bad = am_g != am_r
+    mism = int(bad.sum())
+    if mism:
+        top2 = torch.topk(e_ref[bad], 2, dim=1).values
+        gap = float((top2[:, 0] - top2[:, 1]).max())
+        assert gap <= 2 * err, f"{name}: argmax mismatch away from a tie (gap {gap})"
+    t_err = None
+    if T_gpu is not None:
+        t_err = float((T_gpu.double() - T_ref).abs().max())
+    print(f"{name}: max |d eta| float32 GPU vs float64 = {err:.3e}, "
+          f"argmax mismatches = {mism} of {e_ref.shape[0]}"
+          + (f", max |dT| = {t_err:.3e} K" if t_err is not None else ""))
+    assert err <= ETA_TOL
+    if t_err is not None:
+        assert t_err <= T_TOL
+
+
+def test_directional_solidification_full_size():
+    """64 x 64 x 32 cells, 40 grains, n = 20, isotropic, periodic x/y and
+    Neumann z, T = 1700 K + 1e6 K/m (z - 16 um) - 1e6 * 0.1 t, liquid above
+    T_melt + 1 K set to eta = 0, 200 steps at the stable dt."""
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver, Quench
+    from jax_am_gb300.phase_field.utils import Field
+    from jax_am_gb300.runner import QuenchRun
+    nx, ny, nz = 64, 64, 32
+    pf_args = dict(PF_KEYS, Nx=nx, Ny=ny, Nz=nz, h=1e-6, num_grains=40, num_oris=20,
+                   T_liquidus=1700.0, anisotropy=0.0, force_liquid_zero=True, liquid_shift=1.0,
+                   bc=("periodic", "periodic", "neumann"))
+    poly = Field(pf_args, seed=1)
+    s = PFSolver(pf_args, poly)
+    q = Quench(1700.0, 1e6, 0.1, z0=16e-6)
+    dt = float(np.float32(s.stable_dt()))
+    run = QuenchRun(s, q, dt)
+    run.run(200)
+    a = _oracle_args(pf_args, poly)
+    dirs = _dirs(poly)
+    e = s.ini_cond().double().reshape(nz, ny, nx, -1)
+    zc = 0.5e-6 + 1e-6 * np.arange(nz)
+    t = 0.0
+    for _ in range(200):
+        Tz = np.float32(1700.0 + 1e6 * (zc - 16e-6) - 1e6 * 0.1 * t).astype(np.float64)
+        T3 = torch.tensor(Tz, device="cuda")[:, None, None].expand(nz, ny, nx)
+        e = e + dt * PT.pf_increment(e, T3, a, dirs, bc=(True, True, False))
+        e = torch.where((T3 > 1701.0)[..., None], torch.zeros_like(e), e)
+        t += dt
+    _compare("directional solidification 64x64x32 n=20, 200 steps", run.state, e)
+
+
+def _laser_case(shape, n, grains, aniso, path, steps, seed, name):
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    from jax_am_gb300.phase_field.utils import Field
+    from jax_am_gb300.runner import HeatPFRun
+    from jax_am_gb300.workloads import gamma_args
+    nx, ny, nz = shape
+    pf_args = dict(PF_KEYS, Nx=nx, Ny=ny, Nz=nz, h=1e-6, num_grains=grains, num_oris=n,
+                   T_liquidus=1623.0, anisotropy=aniso)
+    poly = Field(pf_args, seed=seed)
+    s = PFSolver(pf_args, poly)
+    g = gamma_args()
+    run = HeatPFRun(s, g, path)
+    dt = float(np.float32(run.dt))
+    run.run(steps)
+    a = _oracle_args(pf_args, poly)
+    dirs = _dirs(poly)
+    e = s.ini_cond().double().reshape(nz, ny, nx, -1)
+    Tg = torch.full((nz + 2, ny + 2, nx + 2), float(g["T0"]), dtype=torch.float64, device="cuda")
+    path32 = [tuple(float(np.float32(v)) for v in seg) for seg in path]
+
+    def laser(tm):
+        for (t0, t1, x0, y0, x1, y1, P) in path32:
+            if t0 <= tm < t1:
+                f = (tm - t0) / (t1 - t0)
+                return x0 + f * (x1 - x0), y0 + f * (y1 - y0), P
+        return 0.0, 0.0, 0.0
+
+    t = 0.0
+    for _ in range(steps):
+        e, Tg = PT.coupled_step(e, Tg, t, dt, a, g, laser, dirs)
+        t += dt
+    _compare(name, run.state, e, run.T_ghosted[1:-1, 1:-1, 1:-1], Tg[1:-1, 1:-1, 1:-1])
+    return float(Tg.max())
+
+
+def test_single_track_laser_reduced():
+    """Single-track physics (n = 20, A = 0.15, 200 W, r = 50 um, absorptivity
+    0.4, 0.8 m/s, T0 = 300 K) on 100 x 50 x 25 cells, 200 fused steps."""
+    from jax_am_gb300.runner import single_track
+    path = single_track(20e-6, 25e-6, 0.8, 200.0, 1.0)
+    Tmax = _laser_case((100, 50, 25), 20, 60, 0.15, path, 200, 2,
+                       "single track 100x50x25 n=20 A=0.15, 200 steps")
+    assert Tmax > 300.0
+
+
+def test_multi_track_laser_reduced():
+    """Multi-track physics (n = 30, A = 0.15, three tracks 100 um apart at
+    250 W and 1.0 m/s, scanned one after the other) on 80 x 40 x 20 cells
+    with 1 um long tracks 10 um apart, so that all three are scanned in the
+    150 fused steps."""
+    from jax_am_gb300.runner import raster
+    path = raster([10e-6, 20e-6, 30e-6], 1.0, 250.0, 20e-6, 21e-6)
+    _laser_case((80, 40, 20), 30, 40, 0.15, path, 150, 5,
+                "multi track 80x40x20 n=30 A=0.15, 150 steps")
