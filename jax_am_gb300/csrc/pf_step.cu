@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 
 #include "pfg_device.cuh"
@@ -262,6 +263,16 @@ PFConsts make_pf_consts(const pfg_pf_params& p) {
   c.wz = 1.f / (p.h_z * p.h_z);
   c.T_liq = p.T_liquidus;
   c.inv_T_liq = 1.f / p.T_liquidus;
+  {
+    // thresholds of the sign of fl(Tc / T_liq) - 1 (float division, as the
+    // device would do it); a handful of steps from T_liq in each direction
+    const volatile float tl = p.T_liquidus;
+    float hi = tl, lo = tl;
+    for (int i = 0; i < 64 && !((float)(hi / tl) > 1.f); ++i) hi = nextafterf(hi, INFINITY);
+    for (int i = 0; i < 64 && !((float)(lo / tl) < 1.f); ++i) lo = nextafterf(lo, -INFINITY);
+    c.zeta_hi = hi;
+    c.zeta_lo = lo;
+  }
   c.neg_Qg_over_R = -p.Qg / p.gas_const;
   c.L0 = p.L0;
   c.mg_ad = p.m_g / p.ad_hoc;

@@ -96,6 +96,10 @@ __device__ __forceinline__ int bc_index(int i, int n, int periodic) {
 struct PFConsts {
   float wx, wy, wz;          // 1/h^2 per axis
   float T_liq, inv_T_liq;    // liquidus
+  // the float32 quotient Tc / T_liq is above 1 exactly when Tc >= zeta_hi and
+  // below 1 exactly when Tc <= zeta_lo (both found on the host by stepping
+  // through the floats next to T_liq with the same IEEE division)
+  float zeta_hi, zeta_lo;
   float neg_Qg_over_R;       // -Qg / gas_const
   float L0;
   float mg_ad;               // m_g / ad_hoc
@@ -136,12 +140,15 @@ __device__ __forceinline__ TempCoef temp_coefficients(const PFConsts& c, float T
 //    Tc / T_liq is a float32, so x is 0 or at least 2^-24 in magnitude, and
 //    1e10 |x| >= 596: the float32 tanh is exactly +-1 unless x == 0.  zeta is
 //    therefore 0 (x > 0), 1 (x < 0) or 1/2 (x == 0), and NaN propagates.
+//    The sign of x is read from two precomputed thresholds instead of a
+//    division (same result for every float Tc).
 //  * Lg uses the fast exponential (relative error ~1e-6 at the Arrhenius
 //    arguments of this model, |Qg / (R T)| <= 60).
 __device__ __forceinline__ TempCoef temp_coefficients_fast(const PFConsts& c, float T, float dt) {
   const float Tc = (T > 2000.f) ? 2000.f : T;
-  const float x = Tc / c.T_liq - 1.f;
-  const float zeta = (x > 0.f) ? 0.f : (x < 0.f) ? 1.f : (x == 0.f) ? 0.5f : x;
+  const float zeta = (Tc >= c.zeta_hi) ? 0.f
+                     : (Tc <= c.zeta_lo) ? 1.f
+                     : (Tc == Tc) ? 0.5f : Tc;  // Tc == Tc is false only for NaN
   const float Lg = c.L0 * __expf(c.neg_Qg_over_R * rcp_approx(Tc));
   const float om = 1.f - zeta;
   TempCoef r;
