@@ -146,7 +146,7 @@ const char* pfg_status_string(int status);
 const char* pfg_last_cuda_error(void);
 /* sizeof() of the ABI structs, so bindings can check their mirrors:
  * 0 pfg_pf_params, 1 pfg_segment, 2 pfg_heat_params, 3 pfg_clock, 4 pfg_diag,
- * 5 pfg_quench, 6 pfg_batch_job. */
+ * 5 pfg_quench, 6 pfg_batch_job, 7 pfg_grain. */
 int64_t pfg_struct_size(int which);
 
 /* Kernel selection for the stencil steps (process-wide; all compute the same
@@ -280,6 +280,42 @@ int pfg_adjoint_step(const pfg_pf_params* p, const pfg_heat_params* h, const flo
  * and, if lam_seed is not NULL, dJ/d eta = 2 w_i eta_i / N. */
 int pfg_objective(const pfg_pf_params* p, const float* eta, const float* w, double* J,
                   float* lam_seed, void* stream);
+
+/* ---- grain segmentation ---------------------------------------------------
+ * The grains of a solution, as the reference's post-processing finds them
+ * (jax_am/phase_field/utils.py:181-310: compute_edges_in_order, BFS,
+ * get_aspect_ratio_inputs): two face-adjacent cells (no wrap) are in the same
+ * grain when both are solid (T < T_liquidus) and have the same orientation
+ * index.  Each grain record carries the exact integer moments of its cells'
+ * (x, y, z) indices; volume = cells * hx * hy * hz and the PCA aspect ratio
+ * (utils.py:286-310) follow from them on the host.
+ *  ori:           (nz, ny, nx) int32 orientation index per cell (the argmax
+ *                 map, e.g. argmax_out of pfg_pf_diag).
+ *  T:             per-cell (nz, ny, nx) when T_ghosted == 0, else the ghosted
+ *                 heat state.
+ *  grain_of_cell: (nz, ny, nx) int32 grain number per cell (-1 liquid), or NULL.
+ *  grains:        device array of max_grains records, 8-byte aligned; grain g is
+ *                 the g-th grain in increasing order of its smallest cell index
+ *                 (the reference lists grains by orientation first, then in this
+ *                 order: sort the records by (ori, first_cell)).
+ *  num_grains:    device int64 receiving the number of grains; when it exceeds
+ *                 max_grains only the first max_grains records are filled and
+ *                 grain_of_cell may hold numbers >= max_grains: call again with
+ *                 a larger array.
+ *  scratch:       device buffer of at least pfg_grain_scratch_bytes(p) bytes.
+ * Fewer than 2^31 - 2^22 cells. */
+typedef struct pfg_grain {
+  int64_t first_cell;  /* smallest cell index of the grain (where the reference's search starts it) */
+  int32_t ori;         /* its orientation index */
+  int32_t reserved;
+  int64_t cells;       /* number of cells */
+  int64_t sum[3];      /* sums of the cells' x, y, z indices */
+  int64_t sum2[6];     /* sums of xx, yy, zz, xy, xz, yz */
+} pfg_grain;
+int64_t pfg_grain_scratch_bytes(const pfg_pf_params* p);
+int pfg_grains(const pfg_pf_params* p, const int32_t* ori, const float* T, int T_ghosted,
+               int32_t* grain_of_cell, pfg_grain* grains, int64_t max_grains, int64_t* num_grains,
+               void* scratch, int64_t scratch_bytes, void* stream);
 
 /* ---- diagnostics ----------------------------------------------------------
  * The metrics PFSolver.inspect_sol prints (allen_cahn.py:165-180) plus the

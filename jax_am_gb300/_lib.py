@@ -74,6 +74,12 @@ class Diag(ctypes.Structure):
                 ("mass", ctypes.c_double * MAX_ORIS)]
 
 
+class Grain(ctypes.Structure):
+    _fields_ = [("first_cell", ctypes.c_int64), ("ori", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("cells", ctypes.c_int64),
+                ("sum", ctypes.c_int64 * 3), ("sum2", ctypes.c_int64 * 6)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _F = ctypes.c_float
@@ -106,9 +112,12 @@ _PROTOS = {
     "pfg_pf_diag": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, ctypes.c_int64, _P,
                          _P]),
     "pfg_pf_diag_noalloc": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, _P]),
+    "pfg_grain_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(PfParams)]),
+    "pfg_grains": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, ctypes.c_int64, _P, _P,
+                        ctypes.c_int64, _P]),
 }
 _STRUCTS = [(0, PfParams), (1, Segment), (2, HeatParams), (3, Clock), (4, Diag), (5, Quench),
-            (6, BatchJob)]
+            (6, BatchJob), (7, Grain)]
 
 _lib = None
 

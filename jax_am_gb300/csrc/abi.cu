@@ -79,6 +79,7 @@ extern "C" int64_t pfg_struct_size(int which) {
     case 4: return (int64_t)sizeof(pfg_diag);
     case 5: return (int64_t)sizeof(pfg_quench);
     case 6: return (int64_t)sizeof(pfg_batch_job);
+    case 7: return (int64_t)sizeof(pfg_grain);
     default: return -1;
   }
 }

@@ -21,7 +21,10 @@ It restates, in plain NumPy float64, the reference JAX-AM algorithm for:
 * the analytic temperature sources of the phase-field drivers
   (``applications/phase_field/solidification/example.py:21-34``,
   ``applications/phase_field/simple/example.py:21-37``,
-  ``applications/phase_field/multi_scan/example.py:33-84``).
+  ``applications/phase_field/multi_scan/example.py:33-84``);
+* the grain post-processing of ``process_eta``: breadth-first search for
+  same-orientation solid components and their volumes and PCA aspect ratios
+  (``jax_am/phase_field/utils.py:181-310``).
 
 Parity pin: the functions here are checked against golden vectors that the
 reference's own source files produced when run in this container with a
@@ -342,3 +345,72 @@ def read_path(x_corners, y_corners, z_corners, switch, vel, dt):
         t_pre += travel
     return (np.hstack(ts), np.hstack(xs), np.hstack(ys), np.hstack(zs), np.hstack(ps),
             np.vstack(dirs))
+
+
+# ---------------------------------------------------------------------------
+# Grain post-processing (jax_am/phase_field/utils.py:181-310)
+# ---------------------------------------------------------------------------
+
+def grain_components(ori, T, T_liquidus, Nx, Ny, Nz):
+    """Connected same-orientation solid components, numbered as the
+    reference's ``BFS`` + ``combined`` list orders them (``utils.py:
+    219-263``): by orientation, then by discovery in increasing cell index.
+    Solid means ``T < T_liquidus`` (``utils.py:193``); the graph is the
+    6-neighbourhood without wrap (``compute_edges_in_order``,
+    ``utils.py:219-235``).  Returns (labels (N,), -1 in liquid; K)."""
+    from collections import deque
+    N = Nx * Ny * Nz
+    ori = np.asarray(ori).reshape(-1)
+    solid = np.asarray(T).reshape(-1) < T_liquidus
+    comp = -np.ones(N, dtype=np.int64)
+    found = []  # (orientation, first cell) of every component in discovery order
+    for i in range(N):
+        if comp[i] >= 0 or not solid[i]:
+            continue
+        k = len(found)
+        found.append((int(ori[i]), i))
+        comp[i] = k
+        q = deque([i])
+        while q:
+            s = q.popleft()
+            z, r = divmod(s, Nx * Ny)
+            y, x = divmod(r, Nx)
+            for dx, dy, dz in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)):
+                xx, yy, zz = x + dx, y + dy, z + dz
+                if 0 <= xx < Nx and 0 <= yy < Ny and 0 <= zz < Nz:
+                    c = (zz * Ny + yy) * Nx + xx
+                    if comp[c] < 0 and solid[c] and ori[c] == ori[i]:
+                        comp[c] = k
+                        q.append(c)
+    order = sorted(range(len(found)), key=lambda k: found[k])
+    rank = np.empty(len(found), dtype=np.int64)
+    rank[order] = np.arange(len(found))
+    labels = np.where(comp >= 0, rank[np.maximum(comp, 0)], -1)
+    return labels, len(found)
+
+
+def grain_volumes_and_aspect_ratios(labels, K, Nx, Ny, Nz, h):
+    """``get_aspect_ratio_inputs`` + ``compute_aspect_ratios_and_vols``
+    (``utils.py:266-310``): volume = cells x domain_vol / N (uniform cells,
+    ``utils.py:204-205``); grains of fewer than 5 cells get aspect ratio 1;
+    otherwise the PCA explained variances ev (covariance eigenvalues with
+    ddof = 1, descending) of the volume-weighted cell centres give
+    2 sqrt(ev0) / (sqrt(ev1) + sqrt(ev2))."""
+    N = Nx * Ny * Nz
+    vol = (Nx * h) * (Ny * h) * (Nz * h) / N
+    zz, yy, xx = np.meshgrid(np.arange(Nz), np.arange(Ny), np.arange(Nx), indexing="ij")
+    cent = np.stack(((xx.ravel() + 0.5) * h, (yy.ravel() + 0.5) * h, (zz.ravel() + 0.5) * h), axis=1)
+    vols, ars = [], []
+    for k in range(K):
+        cells = np.nonzero(labels == k)[0]
+        vols.append(len(cells) * vol)
+        if len(cells) < 5:
+            ars.append(1.0)
+            continue
+        p = cent[cells] * vol
+        ev = np.sort(np.linalg.eigvalsh(np.cov(p.T, ddof=1)))[::-1]
+        ln = np.sqrt(np.maximum(ev, 0.0))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ars.append(2.0 * ln[0] / (ln[1] + ln[2]))
+    return np.array(vols), np.array(ars)
+

@@ -84,3 +84,27 @@ def test_tsources_match_reference():
     i = int(d["path_i"])
     np.testing.assert_allclose(
         O.T_rosenthal_path(c, 300.0, 0.25, xs[i], ys[i], zs[i], dirs[i]), d["T_path"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("case", ["voronoi_a", "voronoi_b", "voronoi_c", "shapes"])
+def test_grains_match_reference(case):
+    """Grain components, volumes and aspect ratios against the reference's
+    own BFS / PCA code (tests/golden/make_golden_grains.py)."""
+    d = np.load(os.path.join(G, "grains.npz"))
+    Nx, Ny, Nz = (int(v) for v in d[f"{case}_shape"])
+    labels, K = O.grain_components(d[f"{case}_ori"], d[f"{case}_T"], float(d["T_liquidus"]),
+                                   Nx, Ny, Nz)
+    np.testing.assert_array_equal(labels, d[f"{case}_labels"])
+    vols, ars = O.grain_volumes_and_aspect_ratios(labels, K, Nx, Ny, Nz, float(d["h"]))
+    np.testing.assert_allclose(vols, d[f"{case}_vols"], rtol=1e-12)
+    _check_aspect_ratios(ars, d[f"{case}_ars"])
+
+
+def _check_aspect_ratios(ars, ref):
+    """Collinear grains have two zero PCA variances: the ratio is inf, or a
+    huge finite number where rounding left the variances at ~1e-32 of the
+    largest; both count as degenerate (> 1e8).  Others agree to 1e-9."""
+    deg_ref = ~np.isfinite(ref) | (ref > 1e8)
+    deg = ~np.isfinite(ars) | (ars > 1e8)
+    assert np.array_equal(deg, deg_ref)
+    np.testing.assert_allclose(ars[~deg_ref], ref[~deg_ref], rtol=1e-9)
