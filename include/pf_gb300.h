@@ -128,6 +128,34 @@ typedef struct pfg_quench {
   double z_first;  /* centre of the first cell along z [m] */
 } pfg_quench;
 
+/* Analytic moving point source (Rosenthal solution) of the phase-field
+ * drivers (applications/phase_field/simple/example.py:21-37,
+ * simple/example_grf.py:21-46, multi_scan/example.py:33-49):
+ *   T = T_ambient + Q / (2 pi kappa) / R * exp(-vel / (2 alpha) (R + proj)),
+ * R the distance from the source to the cell centre, proj the projection of
+ * (cell centre - source) on the moving direction, then T = min(T, T_clip).
+ * The source state is one record per step: a step that starts with
+ * clk_in->step = k uses record min(k, num_records - 1), so the tool path,
+ * power and speed can follow any schedule (the drivers' read_path samples,
+ * a ramp) with no host work per step. */
+typedef struct pfg_point_source {
+  double t;         /* time of the record [s] (informational) */
+  float x, y, z;    /* source position [m] */
+  float ux, uy, uz; /* unit moving direction */
+  float Q;          /* absorbed power [W] */
+  float vel;        /* speed in the exponent [m/s] */
+} pfg_point_source;
+typedef struct pfg_point_sources {
+  float T_ambient;  /* [K] */
+  float alpha;      /* thermal diffusivity [m^2/s] */
+  float kappa;      /* conductivity [W/(m K)] */
+  float T_clip;     /* clip above this temperature (INFINITY: none) [K] */
+  float x_first, y_first, z_first;  /* centre of cell (0, 0, 0) [m] */
+  int32_t reserved;
+  const pfg_point_source* table;    /* device array of num_records records, 8-byte aligned */
+  int64_t num_records;
+} pfg_point_sources;
+
 /* Results of pfg_pf_diag (device memory, written by the call). */
 typedef struct pfg_diag {
   double energy;                 /* total free energy [J], compensated accumulation */
@@ -146,7 +174,8 @@ const char* pfg_status_string(int status);
 const char* pfg_last_cuda_error(void);
 /* sizeof() of the ABI structs, so bindings can check their mirrors:
  * 0 pfg_pf_params, 1 pfg_segment, 2 pfg_heat_params, 3 pfg_clock, 4 pfg_diag,
- * 5 pfg_quench, 6 pfg_batch_job, 7 pfg_grain. */
+ * 5 pfg_quench, 6 pfg_batch_job, 7 pfg_grain, 8 pfg_point_source,
+ * 9 pfg_point_sources. */
 int64_t pfg_struct_size(int which);
 
 /* Kernel selection for the stencil steps (process-wide; all compute the same
@@ -196,6 +225,19 @@ int pfg_pf_step(const pfg_pf_params* p, const float* eta_in, float* eta_out,
 int pfg_pf_step_quench(const pfg_pf_params* p, const pfg_quench* q, const float* eta_in,
                        float* eta_out, const pfg_clock* clk_in, pfg_clock* clk_out, float dt,
                        void* stream);
+
+/* The same step with T from the moving point source at the start-of-step
+ * step count (the drivers refresh T after each step, simple/example.py:
+ * 62-66, multi_scan/example.py:103-106), evaluated per cell inside the
+ * kernel so that no temperature array exists.  Writes clk_out = {t + dt,
+ * step + 1}; clk_out must not alias clk_in. */
+int pfg_pf_step_point_source(const pfg_pf_params* p, const pfg_point_sources* src,
+                             const float* eta_in, float* eta_out, const pfg_clock* clk_in,
+                             pfg_clock* clk_out, float dt, void* stream);
+/* The (nz, ny, nx) temperature that pfg_pf_step_point_source uses for a step
+ * starting at clk (what the drivers pass to inspect_sol and write_sols). */
+int pfg_point_source_T(const pfg_pf_params* p, const pfg_point_sources* src,
+                       const pfg_clock* clk, float* T_out, void* stream);
 
 /* ---- heat ----------------------------------------------------------------
  * One explicit heat step on the ghosted field, beam at (xl, yl) with the

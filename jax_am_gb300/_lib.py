@@ -74,6 +74,17 @@ class Diag(ctypes.Structure):
                 ("mass", ctypes.c_double * MAX_ORIS)]
 
 
+class PointSourceRecord(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_double)] + [(k, ctypes.c_float) for k in
+                                           ("x", "y", "z", "ux", "uy", "uz", "Q", "vel")]
+
+
+class PointSources(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_float) for k in ("T_ambient", "alpha", "kappa", "T_clip", "x_first",
+                                               "y_first", "z_first")] + [
+        ("reserved", ctypes.c_int32), ("table", ctypes.c_void_p), ("num_records", ctypes.c_int64)]
+
+
 class Grain(ctypes.Structure):
     _fields_ = [("first_cell", ctypes.c_int64), ("ori", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("cells", ctypes.c_int64),
@@ -112,12 +123,16 @@ _PROTOS = {
     "pfg_pf_diag": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, ctypes.c_int64, _P,
                          _P]),
     "pfg_pf_diag_noalloc": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, _P]),
+    "pfg_pf_step_point_source": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PointSources), _P,
+                                      _P, _P, _P, _F, _P]),
+    "pfg_point_source_T": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PointSources), _P, _P,
+                                _P]),
     "pfg_grain_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(PfParams)]),
     "pfg_grains": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, ctypes.c_int64, _P, _P,
                         ctypes.c_int64, _P]),
 }
 _STRUCTS = [(0, PfParams), (1, Segment), (2, HeatParams), (3, Clock), (4, Diag), (5, Quench),
-            (6, BatchJob), (7, Grain)]
+            (6, BatchJob), (7, Grain), (8, PointSourceRecord), (9, PointSources)]
 
 _lib = None
 

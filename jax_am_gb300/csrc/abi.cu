@@ -80,6 +80,8 @@ extern "C" int64_t pfg_struct_size(int which) {
     case 5: return (int64_t)sizeof(pfg_quench);
     case 6: return (int64_t)sizeof(pfg_batch_job);
     case 7: return (int64_t)sizeof(pfg_grain);
+    case 8: return (int64_t)sizeof(pfg_point_source);
+    case 9: return (int64_t)sizeof(pfg_point_sources);
     default: return -1;
   }
 }

@@ -168,5 +168,6 @@ cudaError_t launch_warp_kernel(const StepArgs& a, const TilePlan& t, cudaStream_
 template cudaError_t launch_warp_kernel<kTArray>(const StepArgs&, const TilePlan&, cudaStream_t);
 template cudaError_t launch_warp_kernel<kTHeat>(const StepArgs&, const TilePlan&, cudaStream_t);
 template cudaError_t launch_warp_kernel<kTQuench>(const StepArgs&, const TilePlan&, cudaStream_t);
+template cudaError_t launch_warp_kernel<kTPoint>(const StepArgs&, const TilePlan&, cudaStream_t);
 
 }  // namespace pfg

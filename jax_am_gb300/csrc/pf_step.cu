@@ -139,6 +139,8 @@ pf_zmarch_kernel(const __grid_constant__ StepArgs a) {
   // fused: beam at mid-step; quench: start-of-step time
   float xl = 0.f, yl = 0.f, P = 0.f;
   double t0 = 0.0;
+  pfg_point_source prec{};
+  if constexpr (TSRC == kTPoint) prec = point_record(a.ps, a.clk_in->step);
   if constexpr (TSRC != kTArray) {
     t0 = a.clk_in->t;
     if constexpr (TSRC == kTHeat) laser_at(a.hp, t0 + 0.5 * (double)a.dt, &xl, &yl, &P);
@@ -196,6 +198,9 @@ pf_zmarch_kernel(const __grid_constant__ StepArgs a) {
       float Tc = 0.f;
       if constexpr (TSRC == kTQuench) {
         cc[r * a.tx + xs] = cell_coefficients(plane_tc, s);
+      } else if constexpr (TSRC == kTPoint) {
+        Tc = point_source_T(a.ps, prec, x0 + xs, y0 + r, z);
+        cc[r * a.tx + xs] = cell_coefficients(temp_coefficients(a.pc, Tc, a.dt), s);
       } else {
         Tc = t_cur[(r + 1) * tp + xs + 1];
         cc[r * a.tx + xs] = cell_coefficients(temp_coefficients(a.pc, Tc, a.dt), s);
@@ -281,6 +286,41 @@ PFConsts make_pf_consts(const pfg_pf_params& p) {
   c.liquid_limit = p.T_liquidus + p.liquid_shift;
   c.force = p.force_liquid_zero;
   return c;
+}
+
+PointConsts make_point_consts(const pfg_point_sources& s, const pfg_pf_params& p) {
+  PointConsts c;
+  c.T_ambient = s.T_ambient;
+  c.inv_2pi_kappa = (float)(1.0 / (2.0 * 3.14159265358979323846 * (double)s.kappa));
+  c.inv_2alpha = (float)(1.0 / (2.0 * (double)s.alpha));
+  c.T_clip = s.T_clip;
+  c.x_first = s.x_first; c.y_first = s.y_first; c.z_first = s.z_first;
+  c.hx = p.h_x; c.hy = p.h_y; c.hz = p.h_z;
+  c.table = s.table;
+  c.num_records = s.num_records;
+  return c;
+}
+
+static int check_point_sources(const pfg_point_sources* s) {
+  if (!s || !s->table) return PFG_ERR_NULL;
+  if (reinterpret_cast<uintptr_t>(s->table) % 8 != 0) return PFG_ERR_ALIGN;
+  if (s->num_records < 1 || !(s->alpha > 0.f) || !(s->kappa > 0.f)) return PFG_ERR_PARAM;
+  return PFG_OK;
+}
+
+__global__ void __launch_bounds__(kThreads) point_T_kernel(const PointConsts c,
+                                                           const pfg_clock* clk, float* T,
+                                                           int nx, int ny, int nz) {
+  const pfg_point_source r = point_record(c, clk->step);
+  const int64_t N = (int64_t)nx * ny * nz;
+  const int64_t xy = (int64_t)nx * ny;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int z = (int)(i / xy);
+    const int64_t rem = i - (int64_t)z * xy;
+    const int y = (int)(rem / nx), x = (int)(rem - (int64_t)y * nx);
+    T[i] = point_source_T(c, r, x, y, z);
+  }
 }
 
 HeatConsts make_heat_consts(const pfg_heat_params& h) {
@@ -518,6 +558,42 @@ extern "C" int pfg_pf_step_quench(const pfg_pf_params* p, const pfg_quench* q,
   a.clk_in = clk_in; a.clk_out = clk_out;
   a.q = *q;
   return record_cuda(dispatch<kTQuench>(a, *p, dt, static_cast<cudaStream_t>(stream)));
+}
+
+extern "C" int pfg_pf_step_point_source(const pfg_pf_params* p, const pfg_point_sources* src,
+                                        const float* eta_in, float* eta_out,
+                                        const pfg_clock* clk_in, pfg_clock* clk_out, float dt,
+                                        void* stream) {
+  int st = check_pf_params(p);
+  if (st) return st;
+  st = check_point_sources(src);
+  if (st) return st;
+  if (!eta_in || !eta_out || !clk_in) return PFG_ERR_NULL;
+  if (clk_in == clk_out) return PFG_ERR_PARAM;
+  if (!aligned16(eta_in) || !aligned16(eta_out)) return PFG_ERR_ALIGN;
+  if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  StepArgs a{};
+  a.eta_in = eta_in; a.eta_out = eta_out; a.T = nullptr; a.T_out = nullptr;
+  a.clk_in = clk_in; a.clk_out = clk_out;
+  a.ps = make_point_consts(*src, *p);
+  return record_cuda(dispatch<kTPoint>(a, *p, dt, static_cast<cudaStream_t>(stream)));
+}
+
+extern "C" int pfg_point_source_T(const pfg_pf_params* p, const pfg_point_sources* src,
+                                  const pfg_clock* clk, float* T_out, void* stream) {
+  int st = check_pf_params(p);
+  if (st) return st;
+  st = check_point_sources(src);
+  if (st) return st;
+  if (!clk || !T_out) return PFG_ERR_NULL;
+  if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  const int64_t N = (int64_t)p->nx * p->ny * p->nz;
+  const int64_t want = (N + kThreads - 1) / kThreads;
+  const int64_t cap = (int64_t)device_info().sm_count * 8;
+  const int grid = (int)(want < cap ? want : cap);
+  point_T_kernel<<<grid, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+      make_point_consts(*src, *p), clk, T_out, p->nx, p->ny, p->nz);
+  return record_cuda(cudaGetLastError());
 }
 
 extern "C" int pfg_heat_pf_step(const pfg_pf_params* p, const pfg_heat_params* h,

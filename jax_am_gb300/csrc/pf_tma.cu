@@ -146,6 +146,7 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
 
   __shared__ int s_abort;  // set by any thread whose wait ran out; read after a barrier
   __shared__ double s_t0;
+  __shared__ long long s_step;
   __shared__ float s_beam[3];
   if (threadIdx.x == 0) {
     s_abort = 0;
@@ -161,6 +162,7 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
       }
     }
     s_t0 = t;
+    s_step = (TSRC != kTArray) ? a.clk_in->step : 0;
     if constexpr (TSRC == kTHeat) {
       // beam position and power at mid-step, once per CTA
       laser_at(a.hp, t + 0.5 * (double)a.dt, &s_beam[0], &s_beam[1], &s_beam[2]);
@@ -168,6 +170,9 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   }
   __syncthreads();
   const double t0 = s_t0;
+  // the point source's record for this step (the same for every cell)
+  pfg_point_source prec{};
+  if constexpr (TSRC == kTPoint) prec = point_record(a.ps, s_step);
 
   // ---- staging: plane j (grid plane zb - 1 + j) into ring slot s
   const int cx0 = max(x0 - 1, 0), cx1 = min(xe + 1, a.nx);
@@ -191,7 +196,7 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     for (int q = 0; q < kTQ; ++q) {
       const int i = threadIdx.x + q * NC;
       const int r = fast_div(i, mg), c = i - r * tcols;
-      const bool ok = (TSRC != kTQuench) && i < tcount;
+      const bool ok = (TSRC == kTHeat || TSRC == kTArray) && i < tcount;
       if constexpr (TSRC == kTHeat) {
         t_src[q] = ok ? (y0 + r) * gsy + x0 + c : -1;
         t_dst[q] = r * tp + c;
@@ -313,6 +318,8 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
       }
       TempCoef tc;
       if constexpr (TSRC == kTQuench) tc = plane;
+      else if constexpr (TSRC == kTPoint)
+        tc = temp_coefficients_fast(a.pc, point_source_T(a.ps, prec, c_hx[q], c_hy[q], pz), a.dt);
       else tc = temp_coefficients_fast(a.pc, ts[c_toff[q]], a.dt);
       cb[c_cc[q]] = tma_fold(a.pc, tc, s0 + s1);
     }
@@ -482,6 +489,7 @@ cudaError_t launch_tma_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t
 template cudaError_t launch_tma_kernel<kTArray>(const StepArgs&, const TilePlan&, cudaStream_t);
 template cudaError_t launch_tma_kernel<kTHeat>(const StepArgs&, const TilePlan&, cudaStream_t);
 template cudaError_t launch_tma_kernel<kTQuench>(const StepArgs&, const TilePlan&, cudaStream_t);
+template cudaError_t launch_tma_kernel<kTPoint>(const StepArgs&, const TilePlan&, cudaStream_t);
 
 int read_device_error(int clear) {
   int v = 0;

@@ -282,7 +282,39 @@ __device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc,
   return Tc + dt * ((k * H.inv_rho) * rcp_approx(cp) * (txx + tyy + tzz));
 }
 
+// ---------------------------------------------------------------------------
+// Moving point source (Rosenthal), per cell.
+// ---------------------------------------------------------------------------
+struct PointConsts {
+  float T_ambient, inv_2pi_kappa, inv_2alpha, T_clip;
+  float x_first, y_first, z_first;
+  float hx, hy, hz;
+  const pfg_point_source* table;
+  int64_t num_records;
+};
+
+// The record a step starting at step count `step` uses.
+__device__ __forceinline__ pfg_point_source point_record(const PointConsts& c, int64_t step) {
+  const int64_t k = step < 0 ? 0 : (step < c.num_records ? step : c.num_records - 1);
+  return c.table[k];
+}
+
+// T at the centre of cell (gx, gy, gz) (simple/example.py:28-36,
+// multi_scan/example.py:38-48), float32 with the accurate sqrt and exp.
+__device__ __forceinline__ float point_source_T(const PointConsts& c, const pfg_point_source& r,
+                                                int gx, int gy, int gz) {
+  const float X = fmaf((float)gx, c.hx, c.x_first) - r.x;
+  const float Y = fmaf((float)gy, c.hy, c.y_first) - r.y;
+  const float Z = fmaf((float)gz, c.hz, c.z_first) - r.z;
+  const float R = sqrtf(fmaf(X, X, fmaf(Y, Y, Z * Z)));
+  const float proj = fmaf(X, r.ux, fmaf(Y, r.uy, Z * r.uz));
+  const float T =
+      c.T_ambient + (r.Q * c.inv_2pi_kappa) / R * expf(-(r.vel * c.inv_2alpha) * (R + proj));
+  return (T > c.T_clip) ? c.T_clip : T;  // NaN passes through
+}
+
 HeatConsts make_heat_consts(const pfg_heat_params& h);
+PointConsts make_point_consts(const pfg_point_sources& s, const pfg_pf_params& p);
 PFConsts make_pf_consts(const pfg_pf_params& p);
 
 }  // namespace pfg

@@ -6,7 +6,7 @@
 namespace pfg {
 
 // Where the phase field takes its temperature from.
-enum TSource { kTArray = 0, kTHeat = 1, kTQuench = 2 };
+enum TSource { kTArray = 0, kTHeat = 1, kTQuench = 2, kTPoint = 3 };
 
 struct __align__(16) StepArgs {
   int nx, ny, nz, n;
@@ -28,6 +28,7 @@ struct __align__(16) StepArgs {
   HeatConsts hc;
   pfg_heat_params hp;  // tool path (fused)
   pfg_quench q;        // moving gradient (quench)
+  PointConsts ps;      // moving point source
   float h_z;
   float dirs[3 * PFG_MAX_ORIS * 3];
 };

@@ -171,9 +171,11 @@ __device__ __forceinline__ void warp_unit(const StepArgs& a, int unit, double t0
   const uint64_t magic_tx2 = div_magic(txv + 2);
   const uint64_t magic_txv = div_magic(txv);
 
-  // ---- beam at mid-step
+  // ---- beam at mid-step; point-source record of this step
   float xl = 0.f, yl = 0.f, Pw = 0.f;
   if constexpr (TSRC == kTHeat) laser_at(a.hp, t0 + 0.5 * (double)a.dt, &xl, &yl, &Pw);
+  pfg_point_source prec{};
+  if constexpr (TSRC == kTPoint) prec = point_record(a.ps, a.clk_in->step);
 
   auto stage = [&](int slot, int pz) {
     stage_plane_w<VEC, TSRC>(a, eta_s, T_s, slot, pz, x0, y0, txv, tyv, cx0, row_chunks,
@@ -216,6 +218,8 @@ __device__ __forceinline__ void warp_unit(const StepArgs& a, int unit, double t0
       const float S_ = s0 + s1;
       TempCoef tc;
       if constexpr (TSRC == kTQuench) tc = plane;
+      else if constexpr (TSRC == kTPoint)
+        tc = temp_coefficients_fast(a.pc, point_source_T(a.ps, prec, x0 + c, y0 + r, pz), a.dt);
       else tc = temp_coefficients_fast(a.pc, ts[(r + 1) * (a.tx + 2) + c + 1], a.dt);
       cb[r * a.tx + c] = fold_coefficients(a.pc, tc, S_);
     }

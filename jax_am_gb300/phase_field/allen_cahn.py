@@ -21,6 +21,7 @@ import numpy as np
 import torch
 
 from .. import _lib
+from .point_source import PointSource
 
 _BC = {"neumann": _lib.BC_NEUMANN, "periodic": _lib.BC_PERIODIC}
 
@@ -119,7 +120,9 @@ class PFSolver:
         """One explicit Euler step (``allen_cahn.py:139-143``).
 
         ``state_pre = (eta, t_prev)`` with eta (N, num_oris); ``ode_params =
-        [T]`` with T (N, 1) at the start of the step, or ``[Quench(...)]``.
+        [T]`` with T (N, 1) at the start of the step, or ``[Quench(...)]``, or
+        ``[PointSource(...)]`` (evaluated in the kernel from the record
+        nearest ``t_prev``).
         Returns ``((eta_new, t_crt), eta_new)``.  ``out`` optionally receives
         the result (it must not alias eta)."""
         eta, t_prev = state_pre
@@ -138,6 +141,16 @@ class PFSolver:
             st = self.lib.pfg_pf_step_quench(ctypes.byref(self.params), ctypes.byref(q),
                                               _lib.ptr(eta), _lib.ptr(out), _lib.ptr(clk[0]),
                                               _lib.ptr(clk[1]), dt, _stream())
+        elif isinstance(T, PointSource):
+            clk = self._clocks()
+            clk[0].fill_(0)
+            clk[0].view(torch.float64)[0] = float(t_prev)
+            clk[0][1] = T.index_at(t_prev)
+            src = T.struct(self.params)
+            st = self.lib.pfg_pf_step_point_source(ctypes.byref(self.params), ctypes.byref(src),
+                                                    _lib.ptr(eta), _lib.ptr(out),
+                                                    _lib.ptr(clk[0]), _lib.ptr(clk[1]), dt,
+                                                    _stream())
         else:
             T = as_device_f32(T, (self.N,), "T")
             st = self.lib.pfg_pf_step(ctypes.byref(self.params), _lib.ptr(eta), _lib.ptr(out),

@@ -113,6 +113,39 @@ class QuenchRun(_GraphRun):
         return self.eta[self.cur]
 
 
+class PointSourceRun(_GraphRun):
+    """Phase field under a moving point source (``PointSource``), state
+    resident on the GPU; the device step count selects the source record, so
+    a replayed graph follows the tool path with no host work per step."""
+
+    def __init__(self, solver: PFSolver, source, dt, eta0=None, t0=0.0, step0=0):
+        super().__init__()
+        self.solver = solver
+        self.source = source
+        self.src = source.struct(solver.params)
+        self.dt = float(dt)
+        e0 = solver.ini_cond() if eta0 is None else eta0
+        self.eta = [e0.contiguous().clone(), torch.empty_like(e0)]
+        self.set_time(t0, step0)
+
+    def _launch(self, src):
+        s = self.solver
+        st = s.lib.pfg_pf_step_point_source(ctypes.byref(s.params), ctypes.byref(self.src),
+                                             _lib.ptr(self.eta[src]), _lib.ptr(self.eta[src ^ 1]),
+                                             _lib.ptr(self.clk[src]), _lib.ptr(self.clk[src ^ 1]),
+                                             self.dt, _stream())
+        _lib.check(st, "pfg_pf_step_point_source")
+        self.launches += 1
+
+    @property
+    def state(self):
+        return self.eta[self.cur]
+
+    def T(self):
+        """(N, 1) T of the next step (for inspect_sol / write_sols)."""
+        return self.source.T(self.solver, step=self.steps_taken)
+
+
 def single_track(x_start, y, speed, power, t_end, t_start=0.0):
     """Tool path of one straight track along +x."""
     return [(t_start, t_end, x_start, y, x_start + speed * (t_end - t_start), y, power)]
