@@ -108,3 +108,16 @@ def _check_aspect_ratios(ars, ref):
     deg = ~np.isfinite(ars) | (ars > 1e8)
     assert np.array_equal(deg, deg_ref)
     np.testing.assert_allclose(ars[~deg_ref], ref[~deg_ref], rtol=1e-9)
+
+
+def test_product_read_path_matches_reference():
+    """The tool-path sampler of jax_am_gb300 (host side of the point-source
+    step) against the reference's own read_path output."""
+    from jax_am_gb300.phase_field.point_source import read_path
+    d = np.load(os.path.join(G, "point_sources.npz"))
+    args = dict(vel=float(d["vel"]), dt=float(d["dt"]),
+                laser_path=dict(x_pos=list(d["x_pos"]), y_pos=list(d["y_pos"]),
+                                z_pos=list(d["z_pos"]), switch=list(d["switch"])))
+    out = read_path(args)
+    for a, key in zip(out, ("path_ts", "path_xs", "path_ys", "path_zs", "path_ps", "path_dirs")):
+        np.testing.assert_allclose(a, d[key], rtol=1e-13, atol=1e-18)
