@@ -429,7 +429,7 @@ def time_e2e(solver, g, path, w, steps):
         k = min(check_every, steps - done)
         run.run(k, graph=(k == check_every))
         done += k
-        d = solver.diagnostics(run.state, run.T_ghosted, T_ghosted=True)
+        d = solver.inspect(run.state, run.T_ghosted, T_ghosted=True)
         d2h_diag += 8 * (6 + 64)
         if d["n_nonfinite"]:
             raise ValueError("non-finite eta")
@@ -441,8 +441,9 @@ def time_e2e(solver, g, path, w, steps):
     d2h = eta_out.numel() * 4 + T_out.numel() * 4 + d2h_diag
     return {"value": N * n * steps / el, "unit": UNIT, "h2d_bytes_per_step": h2d / steps,
             "d2h_bytes_per_step": d2h / steps, "seconds": el,
-            "path": "HeatPFRun (public API) + PFSolver.diagnostics every 20 steps, "
-                    "state uploaded from and returned to pinned host memory"}
+            "path": "HeatPFRun (public API) + the inspect_sol metrics (PFSolver.inspect) every "
+                    "20 steps, the reference drivers' check_sol_interval; state uploaded from "
+                    "and returned to pinned host memory"}
 
 
 if __name__ == "__main__":

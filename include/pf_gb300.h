@@ -378,6 +378,14 @@ int pfg_pf_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_
                 const int32_t* argmax0, int32_t* argmax_out,
                 void* scratch, int64_t scratch_bytes, pfg_diag* out, void* stream);
 
+/* Only the metrics of PFSolver.inspect_sol (allen_cahn.py:165-180): argmax
+ * changes, liquid cells, max T, non-finite count and the argmax map; energy
+ * and mass are returned as 0.  Same arguments and scratch as pfg_pf_diag;
+ * one read of eta and no per-orientation sums. */
+int pfg_pf_inspect(const pfg_pf_params* p, const float* eta, const float* T, int T_ghosted,
+                   const int32_t* argmax0, int32_t* argmax_out, void* scratch,
+                   int64_t scratch_bytes, pfg_diag* out, void* stream);
+
 /* ---- diagnostics without allocation -------------------------------------
  * No counterpart in the reference.  The same results as pfg_pf_diag for
  * callers that can neither call cudaMalloc nor pass a scratch buffer: a host

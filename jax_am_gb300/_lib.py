@@ -123,6 +123,8 @@ _PROTOS = {
     "pfg_pf_diag": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, ctypes.c_int64, _P,
                          _P]),
     "pfg_pf_diag_noalloc": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, _P]),
+    "pfg_pf_inspect": (_I, [ctypes.POINTER(PfParams), _P, _P, _I, _P, _P, _P, ctypes.c_int64,
+                            _P, _P]),
     "pfg_pf_step_point_source": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PointSources), _P,
                                       _P, _P, _P, _F, _P]),
     "pfg_point_source_T": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PointSources), _P, _P,

@@ -311,9 +311,104 @@ static void launch_diag_g(const DiagArgs& a, int nb, cudaStream_t s) {
   else pf_diag_kernel<G, false><<<nb, kDiagThreads, 0, s>>>(a);
 }
 
+// ---------------------------------------------------------------------------
+// The metrics of the reference's inspect_sol only (argmax changes, liquid
+// cells, max T, non-finite values).  With no per-orientation sums to keep,
+// one thread takes a whole cell: its orientations are read as 16-byte
+// vectors (several in flight per thread) and scanned in order, so the argmax
+// needs no shuffles.  Partial records as for pf_diag_kernel, with zero energy
+// and mass.
+// ---------------------------------------------------------------------------
+template <bool VEC4>
+__global__ void __launch_bounds__(kDiagThreads) pf_inspect_kernel(const __grid_constant__ DiagArgs a) {
+  constexpr int kWarps = kDiagThreads / 32;
+  __shared__ double s_maxT[kWarps];
+  __shared__ long long s_cnt[kWarps][3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n = a.n;
+  const int64_t ncell = (int64_t)a.nx * a.ny * a.nz;
+  const int64_t xy = (int64_t)a.nx * a.ny;
+  const int64_t gsy = a.nx + 2, gsz = (int64_t)(a.ny + 2) * (a.nx + 2);
+  float maxT = -INFINITY;
+  int changed = 0, liquid = 0, nonfinite = 0;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int64_t ti = c;
+    if (a.T_ghosted) {
+      const int64_t z = c / xy, r = c - z * xy, y = r / a.nx, x = r - y * a.nx;
+      ti = (z + 1) * gsz + (y + 1) * gsy + x + 1;
+    }
+    const float T = a.T[ti];
+    const int a0 = a.argmax0 ? a.argmax0[c] : 0;
+    const float* e = a.eta + c * n;
+    float best = -INFINITY;
+    int bi = 1 << 30;
+    if constexpr (VEC4) {
+      const float4* e4 = reinterpret_cast<const float4*>(e);
+#pragma unroll 4
+      for (int k = 0; k < n / 4; ++k) {
+        const float4 u = __ldg(e4 + k);
+        auto visit = [&](float q, int i) {
+          if (!isfinite(q)) ++nonfinite;
+          if (argmax_better(q, i, best, bi)) { best = q; bi = i; }
+        };
+        visit(u.x, 4 * k);
+        visit(u.y, 4 * k + 1);
+        visit(u.z, 4 * k + 2);
+        visit(u.w, 4 * k + 3);
+      }
+    } else {
+#pragma unroll 4
+      for (int i = 0; i < n; ++i) {
+        const float q = __ldg(e + i);
+        if (!isfinite(q)) ++nonfinite;
+        if (argmax_better(q, i, best, bi)) { best = q; bi = i; }
+      }
+    }
+    if (T >= a.tl_ge) ++liquid;
+    if (T > maxT || isnan(T)) maxT = isnan(maxT) ? maxT : T;
+    if (a.argmax_out) a.argmax_out[c] = bi;
+    if (a.argmax0 && a0 != bi) ++changed;
+  }
+  double mt = (double)maxT;
+  long long c0 = changed, c1 = liquid, c2 = nonfinite;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double om = __shfl_xor_sync(0xffffffffu, mt, o);
+    if (om > mt || isnan(om)) mt = isnan(mt) ? mt : om;
+    c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+    c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+    c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+  }
+  if (lane == 0) {
+    s_maxT[warp] = mt;
+    s_cnt[warp][0] = c0;
+    s_cnt[warp][1] = c1;
+    s_cnt[warp][2] = c2;
+  }
+  __syncthreads();
+  DiagPartial* out = a.partials + blockIdx.x;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) out->mass[i] = 0.0;
+  if (threadIdx.x == 0) {
+    double t2 = -INFINITY;
+    long long d0 = 0, d1 = 0, d2 = 0;
+    for (int w = 0; w < kWarps; ++w) {
+      if (s_maxT[w] > t2 || isnan(s_maxT[w])) t2 = isnan(t2) ? t2 : s_maxT[w];
+      d0 += s_cnt[w][0];
+      d1 += s_cnt[w][1];
+      d2 += s_cnt[w][2];
+    }
+    out->energy = 0.0;
+    out->max_T = t2;
+    out->changed = d0;
+    out->liquid = d1;
+    out->nonfinite = d2;
+  }
+}
+
 int launch_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_ghosted,
                 const int32_t* argmax0, int32_t* argmax_out, void* scratch,
-                pfg_diag* out, cudaStream_t s) {
+                pfg_diag* out, cudaStream_t s, bool full = true) {
   // cell indices are 32-bit in the reduction
   if ((int64_t)p->nx * p->ny * p->nz >= ((int64_t)1 << 31)) return PFG_ERR_SHAPE;
   DiagArgs a{};
@@ -335,7 +430,10 @@ int launch_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_
   a.eta = eta; a.T = T; a.argmax0 = argmax0; a.argmax_out = argmax_out;
   a.partials = static_cast<DiagPartial*>(scratch);
   const int nb = diag_blocks(*p);
-  switch (diag_group(a.n)) {
+  if (!full) {
+    if (a.n % 4 == 0) pf_inspect_kernel<true><<<nb, kDiagThreads, 0, s>>>(a);
+    else pf_inspect_kernel<false><<<nb, kDiagThreads, 0, s>>>(a);
+  } else switch (diag_group(a.n)) {
     case 1: launch_diag_g<1>(a, nb, s); break;
     case 2: launch_diag_g<2>(a, nb, s); break;
     case 4: launch_diag_g<4>(a, nb, s); break;
@@ -356,6 +454,18 @@ using namespace pfg;
 extern "C" int64_t pfg_pf_diag_scratch_bytes(const pfg_pf_params* p) {
   if (check_pf_params(p)) return -1;
   return (int64_t)diag_blocks(*p) * (int64_t)sizeof(DiagPartial);
+}
+
+extern "C" int pfg_pf_inspect(const pfg_pf_params* p, const float* eta, const float* T,
+                              int T_ghosted, const int32_t* argmax0, int32_t* argmax_out,
+                              void* scratch, int64_t scratch_bytes, pfg_diag* out, void* stream) {
+  int st = check_pf_params(p);
+  if (st) return st;
+  if (!eta || !T || !scratch || !out) return PFG_ERR_NULL;
+  if (scratch_bytes < pfg_pf_diag_scratch_bytes(p)) return PFG_ERR_CAPACITY;
+  if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  return launch_diag(p, eta, T, T_ghosted, argmax0, argmax_out, scratch, out,
+                     static_cast<cudaStream_t>(stream), false);
 }
 
 extern "C" int pfg_pf_diag(const pfg_pf_params* p, const float* eta, const float* T,

@@ -179,7 +179,7 @@ class PFSolver:
     def inspect_sol(self, pf_sol, pf_sol0, T, ts, step):
         """Print the reference's run-time metrics (``allen_cahn.py:165-180``)
         from one on-device reduction; raises ValueError on NaN/Inf."""
-        d = self.diagnostics(pf_sol, T, pf_sol0)
+        d = self.inspect(pf_sol, T, pf_sol0)
         print(f"\nstep {step} of {len(ts[1:])}, unix timestamp = {time.time()}")
         print(f"percent of change of orientations = {d['pct_ori_changed']}%")
         print(f"percet of T >= T_liquidus = {d['pct_liquid']}%")
@@ -216,24 +216,29 @@ class PFSolver:
         self._diag(eta, torch.zeros(self.N, device="cuda"), None, out, ghosted=False)
         return out
 
-    def _diag(self, eta, T, argmax0, argmax_out, ghosted):
+    def _diag(self, eta, T, argmax0, argmax_out, ghosted, entry="pfg_pf_diag"):
         if self._diag_scratch is None:
             nbytes = self.lib.pfg_pf_diag_scratch_bytes(ctypes.byref(self.params))
             self._diag_scratch = torch.empty(max(int(nbytes), 16), dtype=torch.uint8,
                                              device="cuda")
             self._diag_out = torch.empty(ctypes.sizeof(_lib.Diag), dtype=torch.uint8,
                                          device="cuda")
-        st = self.lib.pfg_pf_diag(ctypes.byref(self.params), _lib.ptr(eta), _lib.ptr(T),
+        st = getattr(self.lib, entry)(ctypes.byref(self.params), _lib.ptr(eta), _lib.ptr(T),
                                   int(ghosted), _lib.ptr(argmax0), _lib.ptr(argmax_out),
                                   _lib.ptr(self._diag_scratch), self._diag_scratch.numel(),
                                   _lib.ptr(self._diag_out), _stream())
-        _lib.check(st, "pfg_pf_diag")
+        _lib.check(st, entry)
         host = self._diag_out.cpu().numpy()
         return _lib.Diag.from_buffer_copy(host.tobytes())
 
-    def diagnostics(self, eta, T, eta0=None, T_ghosted=False):
+    def inspect(self, eta, T, eta0=None, T_ghosted=False):
+        """The reference's inspect_sol metrics only (argmax changes, liquid
+        fraction, max T, NaN count), one pass over eta on the GPU."""
+        return self.diagnostics(eta, T, eta0, T_ghosted, _entry="pfg_pf_inspect")
+
+    def diagnostics(self, eta, T, eta0=None, T_ghosted=False, _entry="pfg_pf_diag"):
         """Energy, mass, liquid fraction, argmax changes and NaN count of a
-        state, reduced on the GPU (float64 accumulation)."""
+        state, reduced on the GPU (compensated accumulation)."""
         eta = as_device_f32(eta, (self.N, self.n), "eta")
         T = as_device_f32(T, None, "T")
         a0 = None
@@ -242,7 +247,7 @@ class PFSolver:
                 self._argmax0 = self.argmax(as_device_f32(eta0, (self.N, self.n), "eta0"))
                 self._argmax0_src = eta0
             a0 = self._argmax0
-        d = self._diag(eta, T, a0, None, T_ghosted)
+        d = self._diag(eta, T, a0, None, T_ghosted, _entry)
         N = max(int(d.n_cells), 1)
         return {
             "energy": d.energy, "max_T": d.max_T, "n_cells": d.n_cells,

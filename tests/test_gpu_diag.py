@@ -56,3 +56,21 @@ def test_inspect_sol_raises_on_nan(capsys):
     with pytest.raises(ValueError):
         s.inspect_sol(eta, eta, T, np.arange(11), 10)
     assert "percent of change of orientations" in capsys.readouterr().out
+
+
+@pytest.mark.parametrize("shape,n,bc", [((17, 13, 6), 20, "periodic"), ((9, 7, 5), 5, None),
+                                        ((64, 48, 40), 12, None)])
+def test_inspect_matches_full_diagnostics(shape, n, bc):
+    """pfg_pf_inspect (the inspect_sol metrics only) gives the same counts,
+    max T and argmax map as the full reduction, and zero energy and mass."""
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    poly, eta, T, pf_args, oargs, obc = pf_case(shape, n, 0.0, seed=5, bc=bc)
+    s = PFSolver(pf_args, poly)
+    eta0 = np.roll(eta, 1, axis=1)
+    full = s.diagnostics(eta, T, eta0)
+    light = s.inspect(eta, T, eta0)
+    for key in ("n_ori_changed", "n_liquid", "n_nonfinite", "max_T", "n_cells"):
+        assert light[key] == full[key], key
+    assert light["energy"] == 0.0 and not np.any(light["mass"])
+    m = O.inspect(eta, eta0, T, oargs["T_liquidus"])
+    assert light["pct_liquid"] == pytest.approx(m["pct_liquid"], abs=1e-12)
