@@ -189,10 +189,13 @@ class PFSolver:
         return d
 
     def write_sols(self, pf_sol, T, step):
-        """Write T, the argmax orientation map and the liquid mask for step
-        ``step // write_sol_interval`` (``allen_cahn.py:182-210``) as a NumPy
-        ``.npz`` under ``<data_dir>/numpy/pf/sols`` (VTU writing needs meshio,
-        which is not a dependency)."""
+        """Write T and the argmax orientation map for step ``step //
+        write_sol_interval`` (``allen_cahn.py:182-210``): a VTU file
+        ``<data_dir>/vtk/pf/sols/u<k>.vtu`` with cell data ``T`` and
+        ``ori_inds`` (``vtu.write_vtu``; IPF colours are not written), and a
+        NumPy ``.npz`` of T, ori_inds and the liquid mask under
+        ``<data_dir>/numpy/pf/sols`` (what ``grains.process_eta`` reads).
+        Returns the ``.npz`` path."""
         folder = os.path.join(self.pf_args.get("data_dir", "."), "numpy/pf/sols")
         os.makedirs(folder, exist_ok=True)
         k = step // int(self.pf_args.get("write_sol_interval", 1))
@@ -202,6 +205,10 @@ class PFSolver:
         path = os.path.join(folder, f"u{k:03d}.npz")
         np.savez_compressed(path, T=T.cpu().numpy(), ori_inds=argmax.cpu().numpy(),
                             liquid=liquid.cpu().numpy())
+        from .vtu import write_vtu
+        p = self.params
+        write_vtu(os.path.join(self.pf_args.get("data_dir", "."), f"vtk/pf/sols/u{k:03d}.vtu"),
+                  (p.nx, p.ny, p.nz), (p.h_x, p.h_y, p.h_z), {"T": T, "ori_inds": argmax})
         return path
 
     # ---- extensions ---------------------------------------------------------

@@ -129,3 +129,40 @@ class Field:
         if self._centroids is None:
             self._centroids = cell_centroids(self.shape_xyz, self.mesh_h_xyz)
         return self._centroids
+
+
+class StackedField:
+    """Several layers of polycrystal stacked along z (what the reference's
+    ``generate_new_mesh`` builds for multi-layer runs, ``utils.py:151-179``):
+    cells of the lower layers first, the new layer's cells on top (z-major
+    order, so concatenation is stacking); grain directions are those of the
+    newest layer (every layer is built from the same ``ori2``)."""
+
+    def __init__(self, lower, upper):
+        Nx, Ny, Nz_l = lower.shape_xyz
+        Ux, Uy, Nz_u = upper.shape_xyz
+        if (Nx, Ny) != (Ux, Uy) or tuple(lower.mesh_h_xyz) != tuple(upper.mesh_h_xyz):
+            raise ValueError("layers must share Nx, Ny and the cell size")
+        self.shape_xyz = (Nx, Ny, Nz_l + Nz_u)
+        self.mesh_h_xyz = tuple(lower.mesh_h_xyz)
+        self.cell_ori_inds = np.concatenate((lower.cell_ori_inds, upper.cell_ori_inds))
+        self.cell_grain_inds = np.concatenate((lower.cell_grain_inds, upper.cell_grain_inds))
+        self.quaternions = upper.quaternions
+        self.unique_grain_directions = upper.unique_grain_directions
+        self._centroids = None
+
+    @property
+    def centroids(self):
+        if self._centroids is None:
+            self._centroids = cell_centroids(self.shape_xyz, self.mesh_h_xyz)
+        return self._centroids
+
+
+def generate_new_mesh(pf_args, ori2, polycrystal, layer, seed=None):
+    """A new layer of ``pf_args``'s grid (its own Voronoi grains, the
+    orientations ``ori2``) stacked on top of ``polycrystal``, as the
+    reference's ``generate_new_mesh`` (``utils.py:151-179``) does: the new
+    layer's cells sit ``layer`` domain heights up.  Run the stacked
+    polycrystal with ``Nz`` = the total number of cell layers in ``pf_args``."""
+    upper = Field(dict(pf_args), ori2, seed=1 + int(layer) if seed is None else seed)
+    return StackedField(polycrystal, upper)

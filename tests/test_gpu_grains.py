@@ -144,6 +144,10 @@ def test_process_eta_from_written_solution(tmp_path):
     s.write_sols(state[0], T, 13)
     vols, ars = process_eta(pf_args, step=13)
     d = np.load(tmp_path / "numpy/pf/sols/u013.npz")
+    from jax_am_gb300.phase_field.vtu import read_vtu
+    v = read_vtu(str(tmp_path / "vtk/pf/sols/u013.vtu"))
+    np.testing.assert_array_equal(v["ori_inds"], d["ori_inds"])
+    np.testing.assert_array_equal(v["T"], d["T"])
     labels, K = O.grain_components(d["ori_inds"], d["T"], 1623.0, Nx, Ny, Nz)
     ov, oa = O.grain_volumes_and_aspect_ratios(labels, K, Nx, Ny, Nz, 1e-6)
     assert len(vols) == K
