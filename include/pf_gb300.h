@@ -156,6 +156,15 @@ typedef struct pfg_point_sources {
   int64_t num_records;
 } pfg_point_sources;
 
+/* Linear time interpolation between two temperature fields of a coarser
+ * solver, as the coupled driver does (applications/phase_field/coupled/
+ * example.py:38-42): a phase-field step ending at t = clk_in->t + dt uses
+ *   T = r T_past + (1 - r) T_future,  r = (t_future - t) / dt_coarse. */
+typedef struct pfg_interp {
+  double t_future;   /* time of T_future [s] */
+  double dt_coarse;  /* time between T_past and T_future [s] */
+} pfg_interp;
+
 /* Results of pfg_pf_diag (device memory, written by the call). */
 typedef struct pfg_diag {
   double energy;                 /* total free energy [J], compensated accumulation */
@@ -175,7 +184,7 @@ const char* pfg_last_cuda_error(void);
 /* sizeof() of the ABI structs, so bindings can check their mirrors:
  * 0 pfg_pf_params, 1 pfg_segment, 2 pfg_heat_params, 3 pfg_clock, 4 pfg_diag,
  * 5 pfg_quench, 6 pfg_batch_job, 7 pfg_grain, 8 pfg_point_source,
- * 9 pfg_point_sources. */
+ * 9 pfg_point_sources, 10 pfg_interp. */
 int64_t pfg_struct_size(int which);
 
 /* Kernel selection for the stencil steps (process-wide; all compute the same
@@ -238,6 +247,19 @@ int pfg_pf_step_point_source(const pfg_pf_params* p, const pfg_point_sources* sr
  * starting at clk (what the drivers pass to inspect_sol and write_sols). */
 int pfg_point_source_T(const pfg_pf_params* p, const pfg_point_sources* src,
                        const pfg_clock* clk, float* T_out, void* stream);
+
+/* The same step with T interpolated in time between T_past and T_future
+ * (both (nz, ny, nx), the phase-field cell order) at the end-of-step time,
+ * per cell inside the kernel (coupled/example.py:38-42,108-109).  Writes
+ * clk_out = {t + dt, step + 1}; clk_out must not alias clk_in. */
+int pfg_pf_step_interp(const pfg_pf_params* p, const pfg_interp* w, const float* T_past,
+                       const float* T_future, const float* eta_in, float* eta_out,
+                       const pfg_clock* clk_in, pfg_clock* clk_out, float dt, void* stream);
+/* A temperature field of a solver that orders cells (nx, ny, nz), z fastest
+ * (the CFD solver's T[:, :, :, 0]), into the phase-field order (nz, ny, nx):
+ * the coupled driver's convert_temperature (coupled/example.py:31-36). */
+int pfg_transpose_xyz(int32_t nx, int32_t ny, int32_t nz, const float* T_xyz, float* T_zyx,
+                      void* stream);
 
 /* ---- heat ----------------------------------------------------------------
  * One explicit heat step on the ghosted field, beam at (xl, yl) with the

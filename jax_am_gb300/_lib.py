@@ -85,6 +85,10 @@ class PointSources(ctypes.Structure):
         ("reserved", ctypes.c_int32), ("table", ctypes.c_void_p), ("num_records", ctypes.c_int64)]
 
 
+class Interp(ctypes.Structure):
+    _fields_ = [("t_future", ctypes.c_double), ("dt_coarse", ctypes.c_double)]
+
+
 class Grain(ctypes.Structure):
     _fields_ = [("first_cell", ctypes.c_int64), ("ori", ctypes.c_int32),
                 ("reserved", ctypes.c_int32), ("cells", ctypes.c_int64),
@@ -127,6 +131,9 @@ _PROTOS = {
                             _P, _P]),
     "pfg_pf_step_point_source": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PointSources), _P,
                                       _P, _P, _P, _F, _P]),
+    "pfg_pf_step_interp": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(Interp), _P, _P, _P, _P,
+                                _P, _P, _F, _P]),
+    "pfg_transpose_xyz": (_I, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P]),
     "pfg_point_source_T": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PointSources), _P, _P,
                                 _P]),
     "pfg_grain_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(PfParams)]),
@@ -134,7 +141,8 @@ _PROTOS = {
                         ctypes.c_int64, _P]),
 }
 _STRUCTS = [(0, PfParams), (1, Segment), (2, HeatParams), (3, Clock), (4, Diag), (5, Quench),
-            (6, BatchJob), (7, Grain), (8, PointSourceRecord), (9, PointSources)]
+            (6, BatchJob), (7, Grain), (8, PointSourceRecord), (9, PointSources),
+            (10, Interp)]
 
 _lib = None
 

@@ -82,6 +82,7 @@ extern "C" int64_t pfg_struct_size(int which) {
     case 7: return (int64_t)sizeof(pfg_grain);
     case 8: return (int64_t)sizeof(pfg_point_source);
     case 9: return (int64_t)sizeof(pfg_point_sources);
+    case 10: return (int64_t)sizeof(pfg_interp);
     default: return -1;
   }
 }

@@ -169,5 +169,6 @@ template cudaError_t launch_warp_kernel<kTArray>(const StepArgs&, const TilePlan
 template cudaError_t launch_warp_kernel<kTHeat>(const StepArgs&, const TilePlan&, cudaStream_t);
 template cudaError_t launch_warp_kernel<kTQuench>(const StepArgs&, const TilePlan&, cudaStream_t);
 template cudaError_t launch_warp_kernel<kTPoint>(const StepArgs&, const TilePlan&, cudaStream_t);
+template cudaError_t launch_warp_kernel<kTInterp>(const StepArgs&, const TilePlan&, cudaStream_t);
 
 }  // namespace pfg

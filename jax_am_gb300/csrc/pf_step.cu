@@ -201,6 +201,11 @@ pf_zmarch_kernel(const __grid_constant__ StepArgs a) {
       } else if constexpr (TSRC == kTPoint) {
         Tc = point_source_T(a.ps, prec, x0 + xs, y0 + r, z);
         cc[r * a.tx + xs] = cell_coefficients(temp_coefficients(a.pc, Tc, a.dt), s);
+      } else if constexpr (TSRC == kTInterp) {
+        const float w = interp_weight(a.t_future, a.dt_coarse, t0 + (double)a.dt);
+        const int64_t ti = ((int64_t)z * a.ny + y0 + r) * a.nx + x0 + xs;
+        Tc = w * a.T[ti] + (1.f - w) * a.T2[ti];
+        cc[r * a.tx + xs] = cell_coefficients(temp_coefficients(a.pc, Tc, a.dt), s);
       } else {
         Tc = t_cur[(r + 1) * tp + xs + 1];
         cc[r * a.tx + xs] = cell_coefficients(temp_coefficients(a.pc, Tc, a.dt), s);
@@ -577,6 +582,55 @@ extern "C" int pfg_pf_step_point_source(const pfg_pf_params* p, const pfg_point_
   a.clk_in = clk_in; a.clk_out = clk_out;
   a.ps = make_point_consts(*src, *p);
   return record_cuda(dispatch<kTPoint>(a, *p, dt, static_cast<cudaStream_t>(stream)));
+}
+
+extern "C" int pfg_pf_step_interp(const pfg_pf_params* p, const pfg_interp* w,
+                                  const float* T_past, const float* T_future,
+                                  const float* eta_in, float* eta_out, const pfg_clock* clk_in,
+                                  pfg_clock* clk_out, float dt, void* stream) {
+  int st = check_pf_params(p);
+  if (st) return st;
+  if (!w || !T_past || !T_future || !eta_in || !eta_out || !clk_in) return PFG_ERR_NULL;
+  if (clk_in == clk_out) return PFG_ERR_PARAM;
+  if (!(w->dt_coarse > 0.0)) return PFG_ERR_PARAM;
+  if (!aligned16(eta_in) || !aligned16(eta_out)) return PFG_ERR_ALIGN;
+  if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  StepArgs a{};
+  a.eta_in = eta_in; a.eta_out = eta_out; a.T = T_past; a.T2 = T_future; a.T_out = nullptr;
+  a.clk_in = clk_in; a.clk_out = clk_out;
+  a.t_future = w->t_future;
+  a.dt_coarse = w->dt_coarse;
+  return record_cuda(dispatch<kTInterp>(a, *p, dt, static_cast<cudaStream_t>(stream)));
+}
+
+// (nx, ny, nz) z-fastest -> (nz, ny, nx) x-fastest, 32 x 32 tiles of (x, z)
+// through shared memory for each y.
+__global__ void __launch_bounds__(256) transpose_xyz_kernel(int nx, int ny, int nz,
+                                                             const float* __restrict__ src,
+                                                             float* __restrict__ dst) {
+  __shared__ float tile[32][33];
+  const int z0 = blockIdx.x * 32, x0 = blockIdx.y * 32, y = blockIdx.z;
+  for (int k = threadIdx.y; k < 32; k += 8) {  // read rows of x, z fastest
+    const int x = x0 + k, z = z0 + threadIdx.x;
+    if (x < nx && z < nz) tile[k][threadIdx.x] = src[((int64_t)x * ny + y) * nz + z];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += 8) {  // write rows of z, x fastest
+    const int z = z0 + k, x = x0 + threadIdx.x;
+    if (x < nx && z < nz) dst[((int64_t)z * ny + y) * nx + x] = tile[threadIdx.x][k];
+  }
+}
+
+extern "C" int pfg_transpose_xyz(int32_t nx, int32_t ny, int32_t nz, const float* T_xyz,
+                                 float* T_zyx, void* stream) {
+  if (nx < 1 || ny < 1 || nz < 1 || ny > 65535) return PFG_ERR_SHAPE;
+  if (!T_xyz || !T_zyx) return PFG_ERR_NULL;
+  if (T_xyz == T_zyx) return PFG_ERR_PARAM;
+  if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  const dim3 grid((unsigned)((nz + 31) / 32), (unsigned)((nx + 31) / 32), (unsigned)ny);
+  transpose_xyz_kernel<<<grid, dim3(32, 8), 0, static_cast<cudaStream_t>(stream)>>>(nx, ny, nz,
+                                                                                    T_xyz, T_zyx);
+  return record_cuda(cudaGetLastError());
 }
 
 extern "C" int pfg_point_source_T(const pfg_pf_params* p, const pfg_point_sources* src,

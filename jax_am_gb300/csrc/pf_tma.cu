@@ -173,6 +173,8 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   // the point source's record for this step (the same for every cell)
   pfg_point_source prec{};
   if constexpr (TSRC == kTPoint) prec = point_record(a.ps, s_step);
+  float w_past = 0.f;
+  if constexpr (TSRC == kTInterp) w_past = interp_weight(a.t_future, a.dt_coarse, t0 + (double)a.dt);
 
   // ---- staging: plane j (grid plane zb - 1 + j) into ring slot s
   const int cx0 = max(x0 - 1, 0), cx1 = min(xe + 1, a.nx);
@@ -320,6 +322,11 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
       if constexpr (TSRC == kTQuench) tc = plane;
       else if constexpr (TSRC == kTPoint)
         tc = temp_coefficients_fast(a.pc, point_source_T(a.ps, prec, c_hx[q], c_hy[q], pz), a.dt);
+      else if constexpr (TSRC == kTInterp) {
+        const int64_t ti = ((int64_t)pz * a.ny + c_hy[q]) * a.nx + c_hx[q];
+        const float Tp = __ldg(a.T + ti), Tf = __ldg(a.T2 + ti);
+        tc = temp_coefficients_fast(a.pc, w_past * Tp + (1.f - w_past) * Tf, a.dt);
+      }
       else tc = temp_coefficients_fast(a.pc, ts[c_toff[q]], a.dt);
       cb[c_cc[q]] = tma_fold(a.pc, tc, s0 + s1);
     }
@@ -490,6 +497,7 @@ template cudaError_t launch_tma_kernel<kTArray>(const StepArgs&, const TilePlan&
 template cudaError_t launch_tma_kernel<kTHeat>(const StepArgs&, const TilePlan&, cudaStream_t);
 template cudaError_t launch_tma_kernel<kTQuench>(const StepArgs&, const TilePlan&, cudaStream_t);
 template cudaError_t launch_tma_kernel<kTPoint>(const StepArgs&, const TilePlan&, cudaStream_t);
+template cudaError_t launch_tma_kernel<kTInterp>(const StepArgs&, const TilePlan&, cudaStream_t);
 
 int read_device_error(int clear) {
   int v = 0;

@@ -313,6 +313,11 @@ __device__ __forceinline__ float point_source_T(const PointConsts& c, const pfg_
   return (T > c.T_clip) ? c.T_clip : T;  // NaN passes through
 }
 
+// Weight of T_past for a step ending at t_end (coupled/example.py:38-42).
+__device__ __forceinline__ float interp_weight(double t_future, double dt_coarse, double t_end) {
+  return (float)((t_future - t_end) / dt_coarse);
+}
+
 HeatConsts make_heat_consts(const pfg_heat_params& h);
 PointConsts make_point_consts(const pfg_point_sources& s, const pfg_pf_params& p);
 PFConsts make_pf_consts(const pfg_pf_params& p);

@@ -6,7 +6,7 @@
 namespace pfg {
 
 // Where the phase field takes its temperature from.
-enum TSource { kTArray = 0, kTHeat = 1, kTQuench = 2, kTPoint = 3 };
+enum TSource { kTArray = 0, kTHeat = 1, kTQuench = 2, kTPoint = 3, kTInterp = 4 };
 
 struct __align__(16) StepArgs {
   int nx, ny, nz, n;
@@ -29,6 +29,8 @@ struct __align__(16) StepArgs {
   pfg_heat_params hp;  // tool path (fused)
   pfg_quench q;        // moving gradient (quench)
   PointConsts ps;      // moving point source
+  const float* T2;     // interpolation: T_future (T holds T_past)
+  double t_future, dt_coarse;
   float h_z;
   float dirs[3 * PFG_MAX_ORIS * 3];
 };

@@ -176,6 +176,8 @@ __device__ __forceinline__ void warp_unit(const StepArgs& a, int unit, double t0
   if constexpr (TSRC == kTHeat) laser_at(a.hp, t0 + 0.5 * (double)a.dt, &xl, &yl, &Pw);
   pfg_point_source prec{};
   if constexpr (TSRC == kTPoint) prec = point_record(a.ps, a.clk_in->step);
+  float w_past = 0.f;
+  if constexpr (TSRC == kTInterp) w_past = interp_weight(a.t_future, a.dt_coarse, t0 + (double)a.dt);
 
   auto stage = [&](int slot, int pz) {
     stage_plane_w<VEC, TSRC>(a, eta_s, T_s, slot, pz, x0, y0, txv, tyv, cx0, row_chunks,
@@ -220,6 +222,11 @@ __device__ __forceinline__ void warp_unit(const StepArgs& a, int unit, double t0
       if constexpr (TSRC == kTQuench) tc = plane;
       else if constexpr (TSRC == kTPoint)
         tc = temp_coefficients_fast(a.pc, point_source_T(a.ps, prec, x0 + c, y0 + r, pz), a.dt);
+      else if constexpr (TSRC == kTInterp) {
+        const int64_t ti = ((int64_t)pz * a.ny + y0 + r) * a.nx + x0 + c;
+        const float Tp = __ldg(a.T + ti), Tf = __ldg(a.T2 + ti);
+        tc = temp_coefficients_fast(a.pc, w_past * Tp + (1.f - w_past) * Tf, a.dt);
+      }
       else tc = temp_coefficients_fast(a.pc, ts[(r + 1) * (a.tx + 2) + c + 1], a.dt);
       cb[r * a.tx + c] = fold_coefficients(a.pc, tc, S_);
     }

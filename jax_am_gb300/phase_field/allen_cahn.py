@@ -21,6 +21,7 @@ import numpy as np
 import torch
 
 from .. import _lib
+from .coupling import InterpolatedT
 from .point_source import PointSource
 
 _BC = {"neumann": _lib.BC_NEUMANN, "periodic": _lib.BC_PERIODIC}
@@ -122,7 +123,8 @@ class PFSolver:
         ``state_pre = (eta, t_prev)`` with eta (N, num_oris); ``ode_params =
         [T]`` with T (N, 1) at the start of the step, or ``[Quench(...)]``, or
         ``[PointSource(...)]`` (evaluated in the kernel from the record
-        nearest ``t_prev``).
+        nearest ``t_prev``), or ``[InterpolatedT(...)]`` (interpolated in
+        time at ``t_crt`` in the kernel).
         Returns ``((eta_new, t_crt), eta_new)``.  ``out`` optionally receives
         the result (it must not alias eta)."""
         eta, t_prev = state_pre
@@ -139,6 +141,17 @@ class PFSolver:
             clk[0].view(torch.float64)[0] = float(t_prev)
             q = T.struct(self.params.h_z)
             st = self.lib.pfg_pf_step_quench(ctypes.byref(self.params), ctypes.byref(q),
+                                              _lib.ptr(eta), _lib.ptr(out), _lib.ptr(clk[0]),
+                                              _lib.ptr(clk[1]), dt, _stream())
+        elif isinstance(T, InterpolatedT):
+            if T.T_past.numel() != self.N:
+                raise ValueError(f"InterpolatedT holds {T.T_past.numel()} cells, expected {self.N}")
+            clk = self._clocks()
+            clk[0].fill_(0)
+            clk[0].view(torch.float64)[0] = float(t_prev)
+            w = T.struct()
+            st = self.lib.pfg_pf_step_interp(ctypes.byref(self.params), ctypes.byref(w),
+                                              _lib.ptr(T.T_past), _lib.ptr(T.T_future),
                                               _lib.ptr(eta), _lib.ptr(out), _lib.ptr(clk[0]),
                                               _lib.ptr(clk[1]), dt, _stream())
         elif isinstance(T, PointSource):
