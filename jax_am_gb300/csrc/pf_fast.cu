@@ -81,7 +81,8 @@ bool plan_warp_tiles_budget(int nx, int ny, int nz, int n, int sm_count, size_t 
 // as in the batched step, so waves are not counted); max_cells: cap on tile
 // cells.
 bool plan_warp_tiles_ex(int nx, int ny, int nz, int n, int sm_count, size_t budget, int warps,
-                        int ctas_per_sm, int max_cells, TilePlan* out) {
+                        int ctas_per_sm, int max_cells, TilePlan* out, int extra_cells,
+                        bool even_tx) {
   TilePlan t{};
   t.vec = vec_width(n);
   t.tpc = n / t.vec;
@@ -95,11 +96,12 @@ bool plan_warp_tiles_ex(int nx, int ny, int nz, int n, int sm_count, size_t budg
     const int wy = warps / wx;
     const int tx = wx * t.cpw;
     if (!g_tune_wx && wx > 1 && (wx / 2) * t.cpw >= nx) continue;  // a narrower tile covers x
+    if (even_tx && tx % 2 != 0) continue;
     for (int rpw = 1; rpw <= 32; ++rpw) {
       if (g_tune_rpw && rpw != g_tune_rpw) continue;
       const int ty = wy * rpw;
       if (!g_tune_rpw && rpw > 1 && wy * (rpw - 1) >= ny) break;
-      const int pitch = ((tx + 2) * n + 3) / 4 * 4;
+      const int pitch = ((tx + 2 + extra_cells) * n + 3) / 4 * 4;
       const int tslot = ((ty + 2) * (tx + 2) + 3) / 4 * 4;
       const size_t smem = (size_t)t.stages * ((size_t)(ty + 2) * pitch + tslot) * 4 +
                           (size_t)2 * ty * tx * 16;

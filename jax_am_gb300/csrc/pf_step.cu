@@ -476,7 +476,7 @@ static cudaError_t dispatch(StepArgs& a, const pfg_pf_params& p, float dt, cudaS
   TilePlan t;
   const int v = g_kernel_variant;
   if ((v == 0 || v == 3) &&
-      plan_tma_tiles(p.nx, p.ny, p.nz, p.num_oris, d.sm_count, d.smem_per_sm, &t)) {
+      plan_tma_tiles(p.nx, p.ny, p.nz, p.num_oris, p.bc_x, d.sm_count, d.smem_per_sm, &t)) {
     fill_common(a, p, t, dt);
     a.cpw = t.cpw; a.wx = t.wx; a.rpw = t.rpw;
     return launch_tma_kernel<TSRC>(a, t, s);
@@ -508,7 +508,7 @@ extern "C" int pfg_describe_plan(const pfg_pf_params* p, int32_t* out) {
   int kernel;
   const int variant = g_kernel_variant;
   if ((variant == 0 || variant == 3) &&
-      plan_tma_tiles(p->nx, p->ny, p->nz, p->num_oris, d.sm_count, d.smem_per_sm, &t)) {
+      plan_tma_tiles(p->nx, p->ny, p->nz, p->num_oris, p->bc_x, d.sm_count, d.smem_per_sm, &t)) {
     kernel = 3;
   } else if ((variant == 0 || variant == 2 || variant == 3) &&
              plan_warp_tiles(p->nx, p->ny, p->nz, p->num_oris, d.sm_count, d.smem_per_sm, &t)) {

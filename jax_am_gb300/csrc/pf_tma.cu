@@ -116,11 +116,17 @@ __device__ __forceinline__ float4 tma_fold(const PFConsts& c, const TempCoef& tc
 }
 
 // NC threads (256: two CTAs per SM, or 512: one CTA per SM with a tile
-// twice as large).
-template <bool ANISO, int TSRC, int NC>
+// twice as large).  VEC = 4 when num_oris % 4 == 0 (a cell is whole 16-byte
+// vectors); VEC = 2 for other even num_oris with an even nx, even tile
+// widths and Neumann x faces: each halo row is then copied from the even
+// cell at or before x0 - 1 to the even cell at or after xe + 1, so that every
+// bulk copy starts on a 16-byte boundary and moves a multiple of 16 bytes
+// without leaving the grid row, and the tile's first cell sits at position
+// x0 - base of the staged row.
+template <bool ANISO, int TSRC, int NC, int VEC>
 __global__ void __launch_bounds__(NC, NC == 256 ? 2 : 1)
 pf_tma_kernel(const __grid_constant__ StepArgs a) {
-  constexpr int VEC = 4;
+  static_assert(VEC == 4 || VEC == 2, "16- or 8-byte vectors");
   constexpr int kTQ = 3;  // temperature cells staged per thread and plane, at most
   extern __shared__ __align__(128) float smem[];
   const int S = a.stages;
@@ -176,9 +182,21 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   float w_past = 0.f;
   if constexpr (TSRC == kTInterp) w_past = interp_weight(a.t_future, a.dt_coarse, t0 + (double)a.dt);
 
-  // ---- staging: plane j (grid plane zb - 1 + j) into ring slot s
-  const int cx0 = max(x0 - 1, 0), cx1 = min(xe + 1, a.nx);
-  const int dst_cell0 = cx0 - (x0 - 1);
+  // ---- staging: plane j (grid plane zb - 1 + j) into ring slot s.
+  // Cells cx0 .. cx1-1 of each row land at positions dst_cell0 ..; cell x0 of
+  // the tile is at position pos0.
+  int cx0, cx1, dst_cell0, pos0;
+  if constexpr (VEC == 4) {
+    cx0 = max(x0 - 1, 0);
+    cx1 = min(xe + 1, a.nx);
+    dst_cell0 = cx0 - (x0 - 1);
+    pos0 = 1;
+  } else {  // x0, xe and nx even (host checks)
+    cx0 = (x0 >= 2) ? x0 - 2 : 0;
+    cx1 = (xe < a.nx) ? xe + 2 : a.nx;
+    dst_cell0 = 0;
+    pos0 = x0 - cx0;
+  }
   const bool wrap_left = (x0 == 0) && a.bcx == PFG_BC_PERIODIC;
   const bool wrap_right = (xe == a.nx) && a.bcx == PFG_BC_PERIODIC;
   const int rows = tyv + 2;
@@ -248,6 +266,7 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   const bool lane_active = lc < a.cpw;
   const int xs = wxi * a.cpw + (lane_active ? lc : 0);
   const bool col_valid = lane_active && xs < txv;
+  const int xsp = xs + pos0;  // staged-row position of this lane's cell
   const int i0 = kk * VEC;
   // Neumann along x: the edge cell is its own neighbour
   const int gx = x0 + xs;
@@ -283,7 +302,7 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     const int i = threadIdx.x + q * NC;
     c_ok[q] = i < ncell;
     const int r = c_ok[q] ? i / txv : 0, c = c_ok[q] ? i - r * txv : 0;
-    c_eoff[q] = (r + 1) * a.pitch + (c + 1) * n;
+    c_eoff[q] = (r + 1) * a.pitch + (c + pos0) * n;
     c_toff[q] = (r + 1) * tp + c + 1;
     c_cc[q] = r * a.tx + c;
     c_hx[q] = x0 + c;
@@ -308,15 +327,28 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
       const float* ce = es + c_eoff[q];
       float s0 = 0.f, s1 = 0.f;
       int k = 0;
-      for (; k + 8 <= n; k += 8) {
-        const float4 u = *reinterpret_cast<const float4*>(ce + k);
-        const float4 v = *reinterpret_cast<const float4*>(ce + k + 4);
-        s0 = fmaf(u.x, u.x, fmaf(u.y, u.y, fmaf(u.z, u.z, fmaf(u.w, u.w, s0))));
-        s1 = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, s1))));
-      }
-      if (k < n) {
-        const float4 u = *reinterpret_cast<const float4*>(ce + k);
-        s0 = fmaf(u.x, u.x, fmaf(u.y, u.y, fmaf(u.z, u.z, fmaf(u.w, u.w, s0))));
+      if constexpr (VEC == 4) {
+        for (; k + 8 <= n; k += 8) {
+          const float4 u = *reinterpret_cast<const float4*>(ce + k);
+          const float4 v = *reinterpret_cast<const float4*>(ce + k + 4);
+          s0 = fmaf(u.x, u.x, fmaf(u.y, u.y, fmaf(u.z, u.z, fmaf(u.w, u.w, s0))));
+          s1 = fmaf(v.x, v.x, fmaf(v.y, v.y, fmaf(v.z, v.z, fmaf(v.w, v.w, s1))));
+        }
+        if (k < n) {
+          const float4 u = *reinterpret_cast<const float4*>(ce + k);
+          s0 = fmaf(u.x, u.x, fmaf(u.y, u.y, fmaf(u.z, u.z, fmaf(u.w, u.w, s0))));
+        }
+      } else {  // cells start on 8-byte boundaries only
+        for (; k + 4 <= n; k += 4) {
+          const float2 u = *reinterpret_cast<const float2*>(ce + k);
+          const float2 v = *reinterpret_cast<const float2*>(ce + k + 2);
+          s0 = fmaf(u.x, u.x, fmaf(u.y, u.y, s0));
+          s1 = fmaf(v.x, v.x, fmaf(v.y, v.y, s1));
+        }
+        if (k < n) {
+          const float2 u = *reinterpret_cast<const float2*>(ce + k);
+          s0 = fmaf(u.x, u.x, fmaf(u.y, u.y, s0));
+        }
       }
       TempCoef tc;
       if constexpr (TSRC == kTQuench) tc = plane;
@@ -398,7 +430,7 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     int r = r_begin;
     // two rows at a time: rows r-1 .. r+2 of the plane are loaded once
     for (; r + 1 < r_end; r += 2, out_row += 2 * row_elems) {
-      const int off = (r + 1) * a.pitch + (xs + 1) * n + i0;
+      const int off = (r + 1) * a.pitch + xsp * n + i0;
       const int off2 = off + a.pitch;
       VecF<VEC> ym, c, c2, yp2, xm, xp, xm2, xp2, zm, zp, zm2, zp2;
       ym.load(e_cur + off - a.pitch);
@@ -417,7 +449,7 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
       row_out(r + 1, out_row + row_elems, c2, xm2, xp2, c, yp2, zm2, zp2);
     }
     if (r < r_end) {
-      const int off = (r + 1) * a.pitch + (xs + 1) * n + i0;
+      const int off = (r + 1) * a.pitch + xsp * n + i0;
       VecF<VEC> c, xm, xp, ym, yp, zm, zp;
       c.load(e_cur + off);
       xm.load(e_cur + off + off_xm);
@@ -449,16 +481,21 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
 
 int g_tma_consumers = 256;  // threads per CTA: 256 (two CTAs per SM) or 512 (one per SM)
 
-bool plan_tma_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
+bool plan_tma_tiles(int nx, int ny, int nz, int n, int bcx, int sm_count, int max_smem_per_sm,
                     TilePlan* out) {
-  if (n % 4 != 0) return false;
+  // 16-byte vectors, or 8-byte vectors with the aligned-row conditions above
+  const bool vec2 = (n % 4 == 2) && (nx % 2 == 0) && bcx == PFG_BC_NEUMANN &&
+                    g_tma_consumers == 256;
+  if (n % 4 != 0 && !vec2) return false;
   // ghosted temperature offsets are 32-bit in this kernel
   if ((int64_t)(nx + 2) * (ny + 2) * (nz + 2) >= ((int64_t)1 << 31)) return false;
   TilePlan t{};
   const int warps = g_tma_consumers / 32;
   const int ctas = g_tma_consumers == 256 ? 2 : 1;
   const size_t budget = (size_t)max_smem_per_sm / ctas - 2048 - 6 * sizeof(uint64_t) - 64;
-  if (!plan_warp_tiles_ex(nx, ny, nz, n, sm_count, budget, warps, ctas, 2 * g_tma_consumers, &t))
+  // VEC = 2 rows carry up to two more cells (the even-aligned copy range)
+  if (!plan_warp_tiles_ex(nx, ny, nz, n, sm_count, budget, warps, ctas, 2 * g_tma_consumers, &t,
+                          vec2 ? 2 : 0, vec2))
     return false;
   // each thread stages at most three temperature cells of a plane
   if ((t.tx + 2) * (t.ty + 2) > 3 * g_tma_consumers) return false;
@@ -469,9 +506,9 @@ bool plan_tma_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_pe
   return true;
 }
 
-template <bool ANISO, int TSRC, int NC>
+template <bool ANISO, int TSRC, int NC, int VEC>
 static cudaError_t launch_tma_t(const StepArgs& a, const TilePlan& t, cudaStream_t s) {
-  auto k = pf_tma_kernel<ANISO, TSRC, NC>;
+  auto k = pf_tma_kernel<ANISO, TSRC, NC, VEC>;
   static int configured[64] = {0};
   const int dev = device_info().device;
   if (dev < 0 || dev >= 64 || configured[dev] < (int)t.smem) {
@@ -487,10 +524,13 @@ static cudaError_t launch_tma_t(const StepArgs& a, const TilePlan& t, cudaStream
 template <int TSRC>
 cudaError_t launch_tma_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s) {
   if (t.rs == 512)
-    return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 512>(a, t, s)
-                              : launch_tma_t<false, TSRC, 512>(a, t, s);
-  return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 256>(a, t, s)
-                            : launch_tma_t<false, TSRC, 256>(a, t, s);
+    return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 512, 4>(a, t, s)
+                              : launch_tma_t<false, TSRC, 512, 4>(a, t, s);
+  if (t.vec == 2)
+    return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 256, 2>(a, t, s)
+                              : launch_tma_t<false, TSRC, 256, 2>(a, t, s);
+  return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 256, 4>(a, t, s)
+                            : launch_tma_t<false, TSRC, 256, 4>(a, t, s);
 }
 
 template cudaError_t launch_tma_kernel<kTArray>(const StepArgs&, const TilePlan&, cudaStream_t);

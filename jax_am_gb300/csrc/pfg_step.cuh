@@ -44,12 +44,13 @@ bool plan_warp_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
 bool plan_warp_tiles_budget(int nx, int ny, int nz, int n, int sm_count, size_t budget,
                             TilePlan* out);
 bool plan_warp_tiles_ex(int nx, int ny, int nz, int n, int sm_count, size_t budget, int warps,
-                        int ctas_per_sm, int max_cells, TilePlan* out);
+                        int ctas_per_sm, int max_cells, TilePlan* out, int extra_cells = 0,
+                        bool even_tx = false);
 template <int TSRC>
 cudaError_t launch_warp_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);
 void fill_step_args(StepArgs& a, const pfg_pf_params& p, const TilePlan& t, float dt);
 // TMA-fed kernel (pf_tma.cu), num_oris % 4 == 0.
-bool plan_tma_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
+bool plan_tma_tiles(int nx, int ny, int nz, int n, int bcx, int sm_count, int max_smem_per_sm,
                     TilePlan* out);
 template <int TSRC>
 cudaError_t launch_tma_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);

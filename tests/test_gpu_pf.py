@@ -107,6 +107,15 @@ CASES = [
     ((4, 3, 5), 64, 0.15, "periodic", False),
     ((53, 23, 9), 12, 0.15, None, False),
     ((60, 41, 11), 20, 0.15, None, False),
+    # even nx with num_oris % 4 == 2: the TMA kernel's 8-byte-vector rows
+    ((8, 5, 4), 2, 0.15, None, False),
+    ((34, 9, 6), 6, 0.15, None, False),
+    ((40, 7, 5), 10, 0.0, None, True),
+    ((2, 3, 4), 14, 0.15, None, False),
+    ((66, 13, 5), 18, 0.15, None, False),
+    ((100, 11, 4), 22, 0.15, None, False),
+    ((4, 17, 9), 26, 0.15, None, False),
+    ((64, 9, 7), 30, 0.15, ("neumann", "periodic", "periodic"), False),
 ]
 
 
@@ -242,10 +251,14 @@ def test_plans_report_the_kernel_used():
     from jax_am_gb300 import _lib
     from jax_am_gb300.phase_field.allen_cahn import make_pf_params
     lib = _lib.load()
-    for n, kernel in ((20, 3), (12, 3), (10, 2), (30, 2), (7, 2), (33, 1)):
-        poly, eta, T, pf_args, _, _ = pf_case((30, 20, 10), n, 0.15, seed=n)
+    for shape, n, bc, kernel, vec in (((30, 20, 10), 20, None, 3, 4), ((30, 20, 10), 12, None, 3, 4),
+                                      ((30, 20, 10), 10, None, 3, 2), ((30, 20, 10), 30, None, 3, 2),
+                                      ((31, 20, 10), 30, None, 2, 2),
+                                      ((30, 20, 10), 30, "periodic", 2, 2),
+                                      ((30, 20, 10), 7, None, 2, 1), ((30, 20, 10), 33, None, 1, 1)):
+        poly, eta, T, pf_args, _, _ = pf_case(shape, n, 0.15, seed=n, bc=bc)
         plan = _lib.describe_plan(make_pf_params(pf_args, poly))
-        assert plan["kernel"] == kernel, (n, plan)
+        assert plan["kernel"] == kernel and plan["vec"] == vec, (shape, n, bc, plan)
     lib.pfg_set_kernel_variant(1)
     assert _lib.describe_plan(make_pf_params(pf_args, poly))["kernel"] == 1
     lib.pfg_set_kernel_variant(0)
