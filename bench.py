@@ -216,6 +216,57 @@ def time_adjoint():
             "forward_s": t1 - t0, "gradient_s": t2 - t1}
 
 
+def _time_run(run, steps):
+    run.run(min(steps, 20))  # graph capture and warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    run.run(steps)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def time_other_configs(peak):
+    """The other single-solve configurations on the device (graph replay,
+    CUDA events): directional solidification at full size (64 x 64 x 32,
+    40 grains, n = 20, periodic x/y, moving gradient, liquid forcing, its 200
+    steps) and the large multi-track scan (800 x 400 x 200, 20000 grains,
+    n = 30, A = 0.15, fused heat, three 250 W tracks at 1 m/s scanned in turn;
+    200 of its 5000 steps, the per-step cost being the same)."""
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver, Quench
+    from jax_am_gb300.phase_field.utils import Field
+    from jax_am_gb300.runner import HeatPFRun, QuenchRun, raster
+    from jax_am_gb300.workloads import PF_KEYS as WK, gamma_args as wg
+    from jax_am_gb300 import _lib
+    out = {}
+    a1 = dict(WK, Nx=64, Ny=64, Nz=32, h=1e-6, num_grains=40, num_oris=20, T_liquidus=1700.0,
+              anisotropy=0.0, force_liquid_zero=True, liquid_shift=1.0,
+              bc=("periodic", "periodic", "neumann"))
+    s1 = PFSolver(a1, Field(a1, seed=1))
+    run1 = QuenchRun(s1, Quench(1700.0, 1e6, 0.1, z0=16e-6), float(np.float32(s1.stable_dt())))
+    ms = _time_run(run1, 200)
+    N1 = 64 * 64 * 32
+    out["directional_solidification_128K"] = {
+        "steps": 200, "ms_per_step": ms, "cell_ori_updates_per_s": N1 * 20 / (ms / 1e3),
+        "achieved_GBps": N1 * 20 * 8 / (ms / 1e3) / 1e9, "plan": _lib.describe_plan(s1.params)}
+    del run1, s1
+    a5 = dict(WK, Nx=800, Ny=400, Nz=200, h=1e-6, num_grains=20000, num_oris=30,
+              anisotropy=0.15, T_liquidus=1623.0)
+    s5 = PFSolver(a5, Field(a5, seed=5))
+    run5 = HeatPFRun(s5, wg(), raster([100e-6, 200e-6, 300e-6], 1.0, 250.0, 50e-6, 750e-6))
+    ms = _time_run(run5, 200)
+    N5 = 800 * 400 * 200
+    ach = N5 * (2 * 30 * 4 + 8) / (ms / 1e3) / 1e9
+    out["large_multi_track_64M"] = {
+        "steps": 200, "ms_per_step": ms, "cell_ori_updates_per_s": N5 * 30 / (ms / 1e3),
+        "achieved_GBps": ach, "roofline_frac": ach / peak, "plan": _lib.describe_plan(s5.params),
+        "l2": "inputs larger than L2 (eta 7.7 GB per buffer)"}
+    del run5, s5
+    torch.cuda.empty_cache()
+    return out
+
+
 def time_cpu_baseline(w, budget_s=15.0, threads=None, sample=(100, 50, 25), steps_max=50):
     """The float32 PyTorch restatement of the same fused step on the host
     cores, on a reduced grid (bounded sample), in cell*ori updates/s."""
@@ -305,6 +356,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the directional-solidification and 64M multi-track legs")
     ap.add_argument("--profile", action="store_true",
                     help="eager launches only (warmup then steps), for ncu captures")
     args = ap.parse_args()
@@ -383,6 +436,9 @@ def main():
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = time_adjoint()
+    others = None
+    if rank == 0 and not args.no_configs:
+        others = time_other_configs(peak)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -397,7 +453,7 @@ def main():
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": gpu_launches, "clocks": clocks,
             "plan": _lib.describe_plan(solver.params),
-            "serving": serving, "adjoint": adjoint,
+            "serving": serving, "adjoint": adjoint, "other_configs": others,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
