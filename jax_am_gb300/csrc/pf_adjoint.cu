@@ -59,22 +59,52 @@ __device__ __forceinline__ float dzeta_dT(const PFConsts& c, float x) {
   return (x == 0.f) ? -0.5f * 1e10f / c.T_liq : 0.f;
 }
 
-// ---- kernel A: one warp per cell ------------------------------------------
-__global__ void __launch_bounds__(256) adj_pf_local_kernel(const __grid_constant__ AdjArgs a) {
+// Lane layout of kernels A and B: a cell takes tpc = ceil(n / 2) lanes, each
+// lane two consecutive orientations, so a warp holds 32 / tpc cells (for
+// n = 10: six cells, 30 of 32 lanes busy).
+struct AdjLanes {
+  int tpc, cpw, cw, g;
+  bool active;
+};
+__device__ __forceinline__ AdjLanes adj_lanes(int n) {
+  AdjLanes l;
   const int lane = threadIdx.x & 31;
-  const long long ncell = (long long)a.nx * a.ny * a.nz;
-  const long long warp_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  l.tpc = (n + 1) >> 1;
+  l.cpw = 32 / l.tpc;
+  l.cw = lane / l.tpc;
+  l.g = lane - l.cw * l.tpc;
+  l.active = l.cw < l.cpw;
+  return l;
+}
+// Sum of v over the tpc lanes of this lane's cell, returned to every lane of
+// the cell (a guarded shfl-down tree leaves the sum in the cell's lane 0).
+__device__ __forceinline__ float cell_sum(float v, const AdjLanes& l) {
+  for (int o = 1; o < l.tpc; o <<= 1) {
+    const float t = __shfl_down_sync(0xffffffffu, v, o);
+    if (l.g + o < l.tpc) v += t;
+  }
+  const int lane = threadIdx.x & 31;
+  return __shfl_sync(0xffffffffu, v, min(lane - l.g, 31));
+}
+
+// ---- kernel A: u, v, the local term and the temperature sensitivity --------
+__global__ void __launch_bounds__(256) adj_pf_local_kernel(const __grid_constant__ AdjArgs a) {
+  const int ncell = a.nx * a.ny * a.nz;  // host checks < 2^31
   const int n = a.n;
+  const AdjLanes ln = adj_lanes(n);
+  const int warp_id = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
   const float mg = a.pc.mg_ad, kap = a.pc.kappa_ad, A = a.pc.aniso;
-  const int64_t Nn = ncell * n;
-  for (long long c = warp_id; c < ncell; c += nwarps) {
-    const int x = (int)(c % a.nx), y = (int)((c / a.nx) % a.ny), z = (int)(c / ((long long)a.nx * a.ny));
-    const int64_t sy = (int64_t)a.nx * n, sz = (int64_t)a.ny * a.nx * n;
-    const float* e0 = a.eta + c * n;
-    const float* l0 = a.lam_in + c * n;
+  const int64_t Nn = (int64_t)ncell * n;
+  const int xy = a.nx * a.ny;
+  const int64_t sy = (int64_t)a.nx * n, sz = (int64_t)xy * n;
+  const int64_t gsy = a.nx + 2, gsz = (int64_t)(a.ny + 2) * (a.nx + 2);
+  for (int cb = warp_id * ln.cpw; cb < ncell; cb += nwarps * ln.cpw) {
+    const int c = cb + ln.cw;
+    const bool valid = ln.active && c < ncell;
+    const int cc = valid ? c : 0;
+    const int z = cc / xy, r = cc - z * xy, y = r / a.nx, x = r - y * a.nx;
     // temperature-only quantities (as in the forward fast kernels)
-    const int64_t gsy = a.nx + 2, gsz = (int64_t)(a.ny + 2) * (a.nx + 2);
     const float T = a.Tg[(int64_t)(z + 1) * gsz + (int64_t)(y + 1) * gsy + x + 1];
     const bool clipped = T > 2000.f;
     const float Tc = clipped ? 2000.f : T;
@@ -85,23 +115,26 @@ __global__ void __launch_bounds__(256) adj_pf_local_kernel(const __grid_constant
     const float dLg = clipped ? 0.f : Lg * (-a.pc.neg_Qg_over_R) / (Tc * Tc);
     const float dz = clipped ? 0.f : dzeta_dT(a.pc, xz);
     const bool liquid = a.pc.force && T > a.pc.liquid_limit;
+    const int64_t base = (int64_t)z * sz + (int64_t)y * sy + (int64_t)x * n;
     // per-cell sums
     float s = 0.f, ld = 0.f;
-    for (int i = lane; i < n; i += 32) {
-      const float ei = e0[i], li = l0[i];
-      s = fmaf(ei, ei, s);
-      ld = fmaf(li, ei, ld);
-    }
+    if (valid) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      s += __shfl_xor_sync(0xffffffffu, s, o);
-      ld += __shfl_xor_sync(0xffffffffu, ld, o);
+      for (int j = 0; j < 2; ++j) {
+        const int i = 2 * ln.g + j;
+        if (i < n) {
+          const float ei = a.eta[base + i], li = a.lam_in[base + i];
+          s = fmaf(ei, ei, s);
+          ld = fmaf(li, ei, ld);
+        }
+      }
     }
+    s = cell_sum(s, ln);
+    ld = cell_sum(ld, ln);
     const float K = 4.f * s + 2.f * om * om - 1.f;
     const int xm = nbr(x, -1, a.nx, a.bcx), xp = nbr(x, 1, a.nx, a.bcx);
     const int ym = nbr(y, -1, a.ny, a.bcy), yp = nbr(y, 1, a.ny, a.bcy);
     const int zm = nbr(z, -1, a.nz, a.bcz), zp = nbr(z, 1, a.nz, a.bcz);
-    const int64_t base = (int64_t)z * sz + (int64_t)y * sy + (int64_t)x * n;
     const int64_t oxm = (int64_t)z * sz + (int64_t)y * sy + (int64_t)xm * n;
     const int64_t oxp = (int64_t)z * sz + (int64_t)y * sy + (int64_t)xp * n;
     const int64_t oym = (int64_t)z * sz + (int64_t)ym * sy + (int64_t)x * n;
@@ -109,68 +142,75 @@ __global__ void __launch_bounds__(256) adj_pf_local_kernel(const __grid_constant
     const int64_t ozm = (int64_t)zm * sz + (int64_t)y * sy + (int64_t)x * n;
     const int64_t ozp = (int64_t)zp * sz + (int64_t)y * sy + (int64_t)x * n;
     float mu = 0.f;
-    for (int i = lane; i < n; i += 32) {
-      const float e = a.eta[base + i], lam = liquid ? 0.f : a.lam_in[base + i];
-      const float vxm = a.eta[oxm + i], vxp = a.eta[oxp + i];
-      const float vym = a.eta[oym + i], vyp = a.eta[oyp + i];
-      const float vzm = a.eta[ozm + i], vzp = a.eta[ozp + i];
-      const float L = a.pc.wx * ((vxp - e) + (vxm - e)) + a.pc.wy * ((vyp - e) + (vym - e)) +
-                      a.pc.wz * ((vzp - e) + (vzm - e));
-      float an = 1.f, dax = 0.f, day = 0.f, daz = 0.f;
-      if (A > 0.f) {
-        const float ex = vxp - vxm, ey = vyp - vym, ez = vzp - vzm;
-        const float ee = ex * ex + ey * ey + ez * ez;
-        float pbest = 0.f, m = -1.f;
-        int kbest = 0;
+    if (valid) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const float* d = &a.dirs[(k * n + i) * 3];
-          const float pk = d[0] * ex + d[1] * ey + d[2] * ez;
-          if (pk * pk > m) { m = pk * pk; pbest = pk; kbest = k; }
+      for (int j = 0; j < 2; ++j) {
+        const int i = 2 * ln.g + j;
+        if (i >= n) continue;
+        const float e = a.eta[base + i], lam = liquid ? 0.f : a.lam_in[base + i];
+        const float vxm = a.eta[oxm + i], vxp = a.eta[oxp + i];
+        const float vym = a.eta[oym + i], vyp = a.eta[oyp + i];
+        const float vzm = a.eta[ozm + i], vzp = a.eta[ozp + i];
+        const float L = a.pc.wx * ((vxp - e) + (vxm - e)) + a.pc.wy * ((vyp - e) + (vym - e)) +
+                        a.pc.wz * ((vzp - e) + (vzm - e));
+        float an = 1.f, dax = 0.f, day = 0.f, daz = 0.f;
+        if (A > 0.f) {
+          const float ex = vxp - vxm, ey = vyp - vym, ez = vzp - vzm;
+          const float ee = ex * ex + ey * ey + ez * ez;
+          float pbest = 0.f, m = -1.f;
+          int kbest = 0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const float* d = &a.dirs[(k * n + i) * 3];
+            const float pk = d[0] * ex + d[1] * ey + d[2] * ez;
+            if (pk * pk > m) { m = pk * pk; pbest = pk; kbest = k; }
+          }
+          const float c2 = (ee > 0.f) ? m / ee : 1.f;
+          if (c2 < 1.f) {
+            const float s2 = 1.f - c2;
+            an = 1.f + A * (c2 * c2 + s2 * s2);
+            // da/de = A (4 c2 - 2) * 2 (p* d* - c2 e) / ee
+            const float f = A * (4.f * c2 - 2.f) * 2.f / ee;
+            const float* d = &a.dirs[(kbest * n + i) * 3];
+            dax = f * (pbest * d[0] - c2 * ex);
+            day = f * (pbest * d[1] - c2 * ey);
+            daz = f * (pbest * d[2] - c2 * ez);
+          } else {
+            an = 1.f + A;
+          }
         }
-        const float c2 = (ee > 0.f) ? m / ee : 1.f;
-        if (c2 < 1.f) {
-          const float s2 = 1.f - c2;
-          an = 1.f + A * (c2 * c2 + s2 * s2);
-          // da/de = A (4 c2 - 2) * 2 (p* d* - c2 e) / ee
-          const float f = A * (4.f * c2 - 2.f) * 2.f / ee;
-          const float* d = &a.dirs[(kbest * n + i) * 3];
-          dax = f * (pbest * d[0] - c2 * ex);
-          day = f * (pbest * d[1] - c2 * ey);
-          daz = f * (pbest * d[2] - c2 * ez);
-        } else {
-          an = 1.f + A;
-        }
+        const float gg = e * (K - 3.f * e * e);
+        const float Q = Lg * kap;
+        a.u[base + i] = lam * Q * an;
+        a.v[base + i] = lam * Q * L * dax;
+        a.v[Nn + base + i] = lam * Q * L * day;
+        a.v[2 * Nn + base + i] = lam * Q * L * daz;
+        a.loc[base + i] = liquid ? 0.f : -Lg * mg * (lam * (K - 9.f * e * e) + 8.f * e * ld);
+        mu += lam * (dLg * (-mg * gg + kap * an * L) + Lg * mg * 4.f * om * e * dz);
       }
-      const float g = e * (K - 3.f * e * e);
-      const float Q = Lg * kap;
-      a.u[base + i] = lam * Q * an;
-      a.v[base + i] = lam * Q * L * dax;
-      a.v[Nn + base + i] = lam * Q * L * day;
-      a.v[2 * Nn + base + i] = lam * Q * L * daz;
-      a.loc[base + i] = liquid ? 0.f : -Lg * mg * (lam * (K - 9.f * e * e) + 8.f * e * ld);
-      mu += lam * (dLg * (-mg * g + kap * an * L) + Lg * mg * 4.f * om * e * dz);
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mu += __shfl_xor_sync(0xffffffffu, mu, o);
-    if (lane == 0) {
+    mu = cell_sum(mu, ln);
+    if (valid && ln.g == 0) {
       a.muPF[c] = a.dt * mu;
       a.mask[c] = liquid ? 0.f : 1.f;
     }
   }
 }
 
-// ---- kernel B: one warp per cell --------------------------------------------
+// ---- kernel B: the adjoint of the stencil terms, gathered per element --------
 __global__ void __launch_bounds__(256) adj_pf_gather_kernel(const __grid_constant__ AdjArgs a) {
-  const int lane = threadIdx.x & 31;
-  const long long ncell = (long long)a.nx * a.ny * a.nz;
-  const long long warp_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int ncell = a.nx * a.ny * a.nz;
   const int n = a.n;
-  const int64_t Nn = ncell * n;
-  const int64_t sy = (int64_t)a.nx * n, sz = (int64_t)a.ny * a.nx * n;
-  for (long long c = warp_id; c < ncell; c += nwarps) {
-    const int x = (int)(c % a.nx), y = (int)((c / a.nx) % a.ny), z = (int)(c / ((long long)a.nx * a.ny));
+  const AdjLanes ln = adj_lanes(n);
+  const int warp_id = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  const int64_t Nn = (int64_t)ncell * n;
+  const int xy = a.nx * a.ny;
+  const int64_t sy = (int64_t)a.nx * n, sz = (int64_t)xy * n;
+  for (int cb = warp_id * ln.cpw; cb < ncell; cb += nwarps * ln.cpw) {
+    const int c = cb + ln.cw;
+    if (!ln.active || c >= ncell) continue;  // no shuffles below
+    const int z = c / xy, r = c - z * xy, y = r / a.nx, x = r - y * a.nx;
     const int64_t base = (int64_t)z * sz + (int64_t)y * sy + (int64_t)x * n;
     // neighbour offsets and the sign of v at each (odd extension at a Neumann face)
     int64_t off[6];
@@ -188,7 +228,10 @@ __global__ void __launch_bounds__(256) adj_pf_gather_kernel(const __grid_constan
       off[k] = (int64_t)q[2] * sz + (int64_t)q[1] * sy + (int64_t)q[0] * n;
     }
     const float m = a.mask[c];
-    for (int i = lane; i < n; i += 32) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int i = 2 * ln.g + j;
+      if (i >= n) continue;
       const float uc = a.u[base + i];
       const float lapu = a.pc.wx * (a.u[off[0] + i] + a.u[off[1] + i] - 2.f * uc) +
                          a.pc.wy * (a.u[off[2] + i] + a.u[off[3] + i] - 2.f * uc) +
@@ -356,6 +399,9 @@ extern "C" int pfg_adjoint_step(const pfg_pf_params* p, const pfg_heat_params* h
   if (!eta || !Tg || !lam_in || !Tb_in || !lam_out || !Tb_out || !scratch || !grads)
     return PFG_ERR_NULL;
   if (scratch_bytes < pfg_adjoint_scratch_bytes(p)) return PFG_ERR_CAPACITY;
+  // 32-bit cell indices (with room for the grid-stride look-ahead)
+  if ((int64_t)p->nx * p->ny * p->nz >= ((int64_t)1 << 31) - ((int64_t)1 << 22))
+    return PFG_ERR_SHAPE;
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
   AdjArgs a{};
   a.nx = p->nx; a.ny = p->ny; a.nz = p->nz; a.n = p->num_oris;
@@ -390,7 +436,9 @@ extern "C" int pfg_adjoint_step(const pfg_pf_params* p, const pfg_heat_params* h
   for (int i = 0; i < 3 * p->num_oris * 3; ++i) a.dirs[i] = p->grain_dirs[i];
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const DeviceInfo& d = device_info();
-  const int warps_blocks = (int)std::min<int64_t>((N + 7) / 8, (int64_t)d.sm_count * 16);
+  const int cpw = 32 / ((p->num_oris + 1) / 2);  // cells per warp of kernels A and B
+  const int warps_blocks =
+      (int)std::min<int64_t>((N + 8 * cpw - 1) / (8 * cpw), (int64_t)d.sm_count * 16);
   adj_pf_local_kernel<<<warps_blocks, 256, 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return record_cuda(e);
