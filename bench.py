@@ -328,12 +328,13 @@ def run_reference(args):
 def profile_run(args):
     """Eager steps of the laser-track workload, one kernel launch per step:
     ``ncu -k regex:pf_ -s <warmup> -c 1 python bench.py --profile`` captures
-    the first timed launch."""
+    the first timed launch.  ``--profile-oris N`` runs the same grid with N
+    orientations (N = 30: the 8-byte-vector path of the TMA kernel)."""
     import __graft_entry__
     __graft_entry__.build()
     from jax_am_gb300.runner import HeatPFRun
     from jax_am_gb300 import _lib
-    solver, g, path, poly = build_case(WORKLOAD)
+    solver, g, path, poly = build_case(dict(WORKLOAD, num_oris=args.profile_oris))
     run = HeatPFRun(solver, g, path)
     run.run(args.warmup, graph=False)
     torch.cuda.synchronize()
@@ -360,6 +361,8 @@ def main():
                     help="skip the directional-solidification and 64M multi-track legs")
     ap.add_argument("--profile", action="store_true",
                     help="eager launches only (warmup then steps), for ncu captures")
+    ap.add_argument("--profile-oris", type=int, default=WORKLOAD["num_oris"],
+                    help="orientation count of the --profile workload")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.profile:
