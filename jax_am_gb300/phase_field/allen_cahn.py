@@ -305,3 +305,25 @@ def explicit_euler(state_pre, t_crt, solver, ode_params):
     """``explicit_euler(state_pre, t_crt, f, ode_params)`` of the reference
     (``allen_cahn.py:106-114``) with the solver in place of ``f``."""
     return solver.stepper(state_pre, t_crt, ode_params)
+
+
+def rk4(state_pre, t_crt, solver, ode_params):
+    """``rk4(state_pre, t_crt, f, ode_params)`` of the reference
+    (``allen_cahn.py:91-104``, unused by its drivers) with the solver in place
+    of ``f``.  Each stage increment k = h f(y_s) is read off one explicit
+    step from y_s (k = euler(y_s, h) - y_s); the temperature in
+    ``ode_params`` is held over the step as the reference's state_rhs does."""
+    y, t_prev = state_pre
+    y = as_device_f32(y, (solver.N, solver.n), "eta")
+    h = float(t_crt) - float(t_prev)
+
+    def k_of(ys, ts):
+        (e, _), _ = solver.stepper((ys, ts), ts + h, ode_params)
+        return e - ys
+
+    k1 = k_of(y, t_prev)
+    k2 = k_of(y + 0.5 * k1, t_prev + 0.5 * h)
+    k3 = k_of(y + 0.5 * k2, t_prev + 0.5 * h)
+    k4 = k_of(y + k3, t_prev + h)
+    y_crt = y + (k1 + 2.0 * k2 + 2.0 * k3 + k4) / 6.0
+    return (y_crt, t_crt), y_crt

@@ -414,3 +414,13 @@ def grain_volumes_and_aspect_ratios(labels, K, Nx, Ny, Nz, h):
             ars.append(2.0 * ln[0] / (ln[1] + ln[2]))
     return np.array(vols), np.array(ars)
 
+
+
+def rk4(eta, t_prev, t_crt, T, args, grain_dirs=None, bc=(NEUMANN,) * 3):
+    """Fourth-order Runge-Kutta step (``allen_cahn.py:91-104``) with T held."""
+    h = t_crt - t_prev
+    k1 = h * pf_rhs(eta, T, args, grain_dirs, bc)
+    k2 = h * pf_rhs(eta + k1 / 2.0, T, args, grain_dirs, bc)
+    k3 = h * pf_rhs(eta + k2 / 2.0, T, args, grain_dirs, bc)
+    k4 = h * pf_rhs(eta + k3, T, args, grain_dirs, bc)
+    return eta + (k1 + 2 * k2 + 2 * k3 + k4) / 6.0

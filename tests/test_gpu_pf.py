@@ -262,3 +262,24 @@ def test_plans_report_the_kernel_used():
     lib.pfg_set_kernel_variant(1)
     assert _lib.describe_plan(make_pf_params(pf_args, poly))["kernel"] == 1
     lib.pfg_set_kernel_variant(0)
+
+
+@pytest.mark.parametrize("aniso", [0.0, 0.15])
+def test_rk4_vs_oracle(aniso):
+    """The reference's rk4 (allen_cahn.py:91-104) through the GPU step, three
+    steps, against the float64 oracle's RK4."""
+    from jax_am_gb300.phase_field.allen_cahn import rk4
+    poly, eta, T, pf_args, oargs, obc = pf_case((21, 13, 7), 10, aniso, seed=77)
+    s = _solver(pf_args, poly)
+    Td = torch.tensor(T, dtype=torch.float32, device="cuda")
+    state = (torch.tensor(eta, dtype=torch.float32, device="cuda"), 0.0)
+    ref = eta.copy()
+    dt = 1e-8
+    for k in range(3):
+        state, _ = rk4(state, (k + 1) * dt, s, [Td])
+        ref = O.rk4(ref, k * dt, (k + 1) * dt, T, oargs, poly.unique_grain_directions, obc)
+    got = state[0].double().cpu().numpy()
+    err = np.abs(got - ref).max()
+    print(f"rk4 A={aniso}: max |d eta| = {err:.3e}")
+    assert err <= ETA_TOL
+    assert _argmax_mismatch(got, ref) == 0
