@@ -184,7 +184,8 @@ const char* pfg_last_cuda_error(void);
 /* sizeof() of the ABI structs, so bindings can check their mirrors:
  * 0 pfg_pf_params, 1 pfg_segment, 2 pfg_heat_params, 3 pfg_clock, 4 pfg_diag,
  * 5 pfg_quench, 6 pfg_batch_job, 7 pfg_grain, 8 pfg_point_source,
- * 9 pfg_point_sources, 10 pfg_interp. */
+ * 9 pfg_point_sources, 10 pfg_interp, 11 pfg_cfd_grid, 12 pfg_linclip,
+ * 13 pfg_cfd_energy, 14 pfg_cfd_flow, 15 pfg_cfd_stats. */
 int64_t pfg_struct_size(int which);
 
 /* Kernel selection for the stencil steps (process-wide; all compute the same
@@ -430,6 +431,82 @@ int pfg_pf_inspect(const pfg_pf_params* p, const float* eta, const float* T, int
 int pfg_pf_diag_noalloc(const pfg_pf_params* p, const float* eta, const float* T, int T_ghosted,
                         const int32_t* argmax0, int32_t* argmax_out, pfg_diag* out,
                         void* stream);
+
+/* ---- implicit CFD / energy solver (jax_am/cfd/cfd_am.py, AM_3d) ----------
+ * The finite-volume solver the reference's coupled and CFD drivers advance
+ * (applications/phase_field/coupled/example.py:81-111,
+ * applications/cfd/simple/example.py:44-55): per time step an implicit
+ * energy solve (Newton + Jacobi-preconditioned BiCGSTAB), then inside a local
+ * box that follows the laser a projection-method velocity solve (three
+ * momentum solves with Darcy damping and Marangoni shear, a pressure
+ * Poisson) and the explicit convective terms for the next step.
+ *  - float64 throughout (the reference enables jax_enable_x64, cfd_am.py:10).
+ *  - Fields are (nx, ny, nz) C order, z fastest -- the reference's
+ *    (Nx, Ny, Nz, 1) arrays; vel, conv and grad_p0 are (nx, ny, nz, 3).
+ *  - The solves are iterative with data-dependent iteration counts, so these
+ *    entry points synchronise with `stream` to read convergence flags (a few
+ *    bytes per chunk of iterations); they return when the step's results
+ *    are complete on the device.
+ *  - `ws` is caller-owned device scratch of pfg_cfd_workspace_bytes() bytes,
+ *    8-byte aligned; its contents are not preserved between calls. */
+typedef struct pfg_cfd_grid {
+  int32_t nx, ny, nz, pad;
+  double dx, dy, dz;             /* cell size: domain / N (cfd_am.py:677-679) */
+  double lx, ly, lz;             /* domain lengths: the last mesh node (cfd_am.py:672-674) */
+} pfg_cfd_grid;
+
+typedef struct pfg_linclip {     /* a * clip(T, lo, hi) + b: the drivers' cp(T) and k(T) */
+  double a, b, lo, hi;
+} pfg_linclip;
+
+typedef struct pfg_cfd_energy {  /* energy_eqn + AM_3d's energy boundary condition */
+  pfg_linclip cp, k;
+  double rho, latent_heat, Ts, Tl, dt;
+  double T_ref, h_conv, emissivity, sigma;  /* top face: -h (T - T_ref) - sigma eps (T^4 - T_ref^4) */
+  int32_t heat_source;           /* 0: Gaussian surface flux, 1: Gaussian cylinder body source */
+  int32_t max_newton;            /* solver_nonlinear max_it (50) */
+  double P, eta, rb, phi, speed; /* laser power (already 0 after t_OFF), absorptivity, radius, ... */
+  double xl, yl, zl;             /* beam position at the step's time (AM_3d.toolpath) */
+  double newton_tol;             /* solver_nonlinear tol (1e-5) */
+} pfg_cfd_energy;
+
+typedef struct pfg_cfd_flow {    /* velocity_eqn + AM_3d's moving box */
+  double rho, visco, dt, marangoni, Ts, Tl;
+  int32_t x0, y0, z0, pad;       /* the local box's origin in the global grid */
+} pfg_cfd_flow;
+
+typedef struct pfg_cfd_stats {   /* iteration counts of the last call (-10/-11: breakdown) */
+  int32_t newton_iters, pad;
+  int64_t energy_krylov;         /* BiCGSTAB iterations summed over the Newton steps */
+  int64_t momentum_krylov[3];
+  int64_t pressure_krylov;
+} pfg_cfd_stats;
+
+/* Scratch bytes for a global grid and a local box (either solve). */
+int64_t pfg_cfd_workspace_bytes(const pfg_cfd_grid* global, const pfg_cfd_grid* local);
+
+/* energy_eqn.update + solver_nonlinear (cfd_am.py:516-525, 780-812) with
+ * AM_3d's boundary condition and heat source at the step's time
+ * (cfd_am.py:223-235, 325-358): T_out = the new temperature from T0 (the
+ * previous one; its top layer gives the radiation/convection flux) and the
+ * explicit convection conv_T. */
+int pfg_cfd_energy_solve(const pfg_cfd_grid* g, const pfg_cfd_energy* e, const double* T0,
+                         const double* conv_T, double* T_out, void* ws, int64_t ws_bytes,
+                         pfg_cfd_stats* stats, void* stream);
+
+/* solidID = max(solidID, fluid fraction of T) (cfd_am.py:172-175, 360-363). */
+int pfg_cfd_solid_update(const pfg_cfd_grid* g, double Ts, double Tl, const double* T,
+                         double* solidID, void* stream);
+
+/* velocity_eqn.update on the local box at f->x0/y0/z0 (cfd_am.py:557-590,
+ * 287-323) followed by update_convective_terms (cfd_am.py:254-259): reads T
+ * and the box's vel, conv and grad_p0 from the global arrays, writes the
+ * box's vel, grad_p0, conv and conv_T back.  The convective terms use the
+ * global cell size, the solves the local box's (as the reference does). */
+int pfg_cfd_flow_step(const pfg_cfd_grid* global, const pfg_cfd_grid* local,
+                      const pfg_cfd_flow* f, const double* T, double* vel, double* conv,
+                      double* grad_p0, double* conv_T, void* ws, int64_t ws_bytes,
+                      pfg_cfd_stats* stats, void* stream);
 
 #ifdef __cplusplus
 }

@@ -95,6 +95,36 @@ class Grain(ctypes.Structure):
                 ("sum", ctypes.c_int64 * 3), ("sum2", ctypes.c_int64 * 6)]
 
 
+class CfdGrid(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("pad", ctypes.c_int32)] + [(k, ctypes.c_double) for k in
+                                            ("dx", "dy", "dz", "lx", "ly", "lz")]
+
+
+class LinClipC(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("a", "b", "lo", "hi")]
+
+
+class CfdEnergy(ctypes.Structure):
+    _fields_ = ([("cp", LinClipC), ("k", LinClipC)]
+                + [(k, ctypes.c_double) for k in ("rho", "latent_heat", "Ts", "Tl", "dt", "T_ref",
+                                                  "h_conv", "emissivity", "sigma")]
+                + [("heat_source", ctypes.c_int32), ("max_newton", ctypes.c_int32)]
+                + [(k, ctypes.c_double) for k in ("P", "eta", "rb", "phi", "speed", "xl", "yl",
+                                                  "zl", "newton_tol")])
+
+
+class CfdFlow(ctypes.Structure):
+    _fields_ = ([(k, ctypes.c_double) for k in ("rho", "visco", "dt", "marangoni", "Ts", "Tl")]
+                + [(k, ctypes.c_int32) for k in ("x0", "y0", "z0", "pad")])
+
+
+class CfdStats(ctypes.Structure):
+    _fields_ = [("newton_iters", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("energy_krylov", ctypes.c_int64), ("momentum_krylov", ctypes.c_int64 * 3),
+                ("pressure_krylov", ctypes.c_int64)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _F = ctypes.c_float
@@ -134,6 +164,14 @@ _PROTOS = {
     "pfg_pf_step_interp": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(Interp), _P, _P, _P, _P,
                                 _P, _P, _F, _P]),
     "pfg_transpose_xyz": (_I, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P, _P, _P]),
+    "pfg_cfd_workspace_bytes": (ctypes.c_int64, [ctypes.POINTER(CfdGrid), ctypes.POINTER(CfdGrid)]),
+    "pfg_cfd_energy_solve": (_I, [ctypes.POINTER(CfdGrid), ctypes.POINTER(CfdEnergy), _P, _P, _P,
+                                  _P, ctypes.c_int64, ctypes.POINTER(CfdStats), _P]),
+    "pfg_cfd_solid_update": (_I, [ctypes.POINTER(CfdGrid), ctypes.c_double, ctypes.c_double, _P,
+                                  _P, _P]),
+    "pfg_cfd_flow_step": (_I, [ctypes.POINTER(CfdGrid), ctypes.POINTER(CfdGrid),
+                               ctypes.POINTER(CfdFlow), _P, _P, _P, _P, _P, _P, ctypes.c_int64,
+                               ctypes.POINTER(CfdStats), _P]),
     "pfg_point_source_T": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(PointSources), _P, _P,
                                 _P]),
     "pfg_grain_scratch_bytes": (ctypes.c_int64, [ctypes.POINTER(PfParams)]),
@@ -142,7 +180,8 @@ _PROTOS = {
 }
 _STRUCTS = [(0, PfParams), (1, Segment), (2, HeatParams), (3, Clock), (4, Diag), (5, Quench),
             (6, BatchJob), (7, Grain), (8, PointSourceRecord), (9, PointSources),
-            (10, Interp)]
+            (10, Interp), (11, CfdGrid), (12, LinClipC), (13, CfdEnergy), (14, CfdFlow),
+            (15, CfdStats)]
 
 _lib = None
 

@@ -83,6 +83,11 @@ extern "C" int64_t pfg_struct_size(int which) {
     case 8: return (int64_t)sizeof(pfg_point_source);
     case 9: return (int64_t)sizeof(pfg_point_sources);
     case 10: return (int64_t)sizeof(pfg_interp);
+    case 11: return (int64_t)sizeof(pfg_cfd_grid);
+    case 12: return (int64_t)sizeof(pfg_linclip);
+    case 13: return (int64_t)sizeof(pfg_cfd_energy);
+    case 14: return (int64_t)sizeof(pfg_cfd_flow);
+    case 15: return (int64_t)sizeof(pfg_cfd_stats);
     default: return -1;
   }
 }

@@ -78,10 +78,9 @@ class Mesh:
         self.D = np.array([-dx, dx, -dy, dy, -dz, dz])
         self.dS = np.array([-dy * dz, dy * dz, -dz * dx, dz * dx, -dx * dy, dx * dy])
         self.cell_num = int(np.prod(self.shape))
-        Nx, Ny, Nz = self.shape
-        xs = (np.arange(Nx) + 0.5) * dx
-        ys = (np.arange(Ny) + 0.5) * dy
-        zs = (np.arange(Nz) + 0.5) * dz
+        # cell centres: midpoints of numpy.linspace nodes (cfd_am.py:672-680)
+        xs, ys, zs = ((n[1:] + n[:-1]) / 2 for n in
+                      (np.linspace(0.0, L, k + 1) for L, k in zip(self.domain, self.shape)))
         X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
         self.Xc = np.stack((X, Y, Z), axis=3).reshape(-1, 3)
 
