@@ -216,6 +216,60 @@ def time_adjoint():
             "forward_s": t1 - t0, "gradient_s": t2 - t1}
 
 
+def time_cfd(steps=20, warmup=3, cpu=False):
+    """The implicit CFD solver (``AM_3d``, float64) on the reference's
+    standalone CFD driver configuration (``workloads.cfd_simple_case``):
+    ``warmup`` steps (the melt pool forms and the flow starts), then
+    ``steps`` timed steps with CUDA events around ``time_integration`` (which
+    reads only convergence flags on the host).  ``cpu``: also time one step
+    of the float64 CPU oracle from the same state (tens of seconds)."""
+    from jax_am_gb300.cfd import cfd_am as G
+    from jax_am_gb300.workloads import cfd_simple_case
+    s = G.AM_3d(cfd_simple_case())
+    for _ in range(warmup):
+        s.time_integration()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    its = []
+    e0.record()
+    for _ in range(steps):
+        s.time_integration()
+        its.append(s.iterations())
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    mean = lambda xs: sum(xs) / len(xs)  # noqa: E731
+    out = {"workload": "cfd_simple_2M: 464x93x46 cells, 348x46x18 flow box, 100 W at 0.5 m/s "
+                       "(applications/cfd/simple), float64",
+           "warmup_steps": warmup, "steps": steps, "ms_per_step": ms,
+           "cells_per_s": 464 * 93 * 46 / (ms / 1e3),
+           "newton_per_step": mean([i["newton"] for i in its]),
+           "energy_krylov_per_step": mean([i["energy_krylov"] for i in its]),
+           "momentum_krylov_per_step": mean([sum(i["momentum_krylov"]) for i in its]),
+           "pressure_krylov_per_step": mean([i["pressure_krylov"] for i in its]),
+           "T_max": float(s.T.max()), "vel_max": float(s.vel.abs().max())}
+    if cpu:
+        import numpy as np
+        from oracle import cfd_oracle as C
+        a = cfd_simple_case()
+        mesh, ml = a["mesh"], a["mesh_local"]
+        o = C.AM3d(dict(a, cp=C.LinClip(*G.linear_clip_params(a["cp"])),
+                        k=C.LinClip(*G.linear_clip_params(a["k"]))),
+                   C.Mesh(mesh.domain, mesh.shape), C.Mesh(ml.domain, ml.shape))
+        for name in ("T", "vel", "conv", "grad_p0"):
+            setattr(o, name, getattr(s, name).cpu().numpy().reshape(getattr(o, name).shape))
+        o.conv_T = s.conv_T.cpu().numpy()[..., 0]
+        o.solidID = s.solidID.cpu().numpy()[..., 0]
+        o.t = s.t
+        t0 = time.perf_counter()
+        o.time_integration()
+        cpu_s = time.perf_counter() - t0
+        out["cpu_oracle"] = {"s_per_step": cpu_s, "kind": "port", "cores": 1,
+                             "sample": "one step of the float64 NumPy oracle from the GPU "
+                                       "run's state", "iterations": o.last_iters}
+    return out
+
+
 def _time_run(run, steps):
     run.run(min(steps, 20))  # graph capture and warm-up
     torch.cuda.synchronize()
@@ -357,6 +411,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-cfd", action="store_true", help="skip the implicit CFD solver leg")
+    ap.add_argument("--cfd-cpu", action="store_true",
+                    help="also time one step of the float64 CPU oracle of the CFD solver")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the directional-solidification and 64M multi-track legs")
     ap.add_argument("--profile", action="store_true",
@@ -442,6 +499,9 @@ def main():
     others = None
     if rank == 0 and not args.no_configs:
         others = time_other_configs(peak)
+    cfd = None
+    if rank == 0 and not args.no_cfd:
+        cfd = time_cfd(cpu=args.cfd_cpu)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -457,6 +517,7 @@ def main():
             "gpu_launches": gpu_launches, "clocks": clocks,
             "plan": _lib.describe_plan(solver.params),
             "serving": serving, "adjoint": adjoint, "other_configs": others,
+            "cfd_am3d": cfd,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

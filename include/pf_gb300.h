@@ -207,8 +207,10 @@ int pfg_device_error(int clear);
  * (value 0 restores the automatic choice): key 0 = warps along x (1 .. 16),
  * 1 = rows per warp (1..32), 2 = shared-memory plane slots (4..6),
  * 3 = z chunks per tile column, 5 = consumer threads of the TMA-fed kernel
- * (256: two CTAs per SM; 512: one larger CTA per SM).  Process-wide; results
- * do not change. */
+ * (256: two CTAs per SM; 512: one larger CTA per SM), 6 = cells per thread of
+ * the CFD solver's kernels (1..16, default 4).  Process-wide; the stencil
+ * steps' results do not change; the CFD solver's dot products are summed in
+ * another order (float64 rounding only). */
 int pfg_tune(int key, int value);
 
 /* The launch plan a step with these parameters would use on the current

@@ -23,10 +23,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "pfg_host.h"
 
 namespace pfg {
+int g_cfd_cells_per_thread = 4;  // pfg_tune key 6
+
 namespace cfd {
 
 constexpr int kThreads = 256;
@@ -79,11 +82,14 @@ __device__ __forceinline__ bool on_face(const Dims& d, int i, int j, int k, int 
     default: return k == d.nz - 1;
   }
 }
+// cell -> (i, j, k); the host keeps n below 2^31, so 32-bit division suffices
 __device__ __forceinline__ void ijk(const Dims& d, long long c, int& i, int& j, int& k) {
-  k = (int)(c % d.nz);
-  const long long r = c / d.nz;
-  j = (int)(r % d.ny);
-  i = (int)(r / d.ny);
+  const unsigned cu = (unsigned)c, nz = (unsigned)d.nz, ny = (unsigned)d.ny;
+  const unsigned r = cu / nz;
+  k = (int)(cu - r * nz);
+  const unsigned q = r / ny;
+  j = (int)(r - q * ny);
+  i = (int)q;
 }
 
 // np.clip: min(max(T, lo), hi), NaN passes through
@@ -132,18 +138,25 @@ __device__ double sum_partials(const double* P, int nb, double* sh) {
 }
 
 // ---- BiCGSTAB --------------------------------------------------------------
+// Scalars live in device memory.  A dot product is a partial sum per block;
+// the block that completes the slot's counter (an atomic increment after
+// its partial is fenced) adds the partials in block order and stores the
+// result, so every value is reduced once and in a fixed order.
 struct KState {
   double atol2, rho, alpha, omega;  // previous iteration's scalars
   double rho_new;                   // <rhat, r> for the coming iteration
   double rs;                        // <r, r>
+  double alpha_cur, ss, omega_cur;  // this iteration's alpha, <s, s>, omega
+  double bb;                        // <b, b> (setup) or a residual norm^2
   long long k, maxiter;
   int done, pad;
+  unsigned cnt[8];                  // last-block counters, one per slot
 };
 enum { P_RQ = 0, P_SS, P_TS, P_TT, P_RR, P_RHR, P_BB, P_AUX };
 
 struct Work {
   double* vals;  // 7 n
-  double* diag;  // n
+  double* diag;  // n: Jacobi reciprocals 1 / precond_values
   double* b;
   double* x;
   double* r;
@@ -159,14 +172,64 @@ struct Work {
   KState* st;
 };
 
+// Blocks for n cells: about four cells per thread, at most four blocks per
+// SM.  GB300 issues about two float64 FMAs per clock per SM, so a block's
+// reduction tree (a few float64 adds per lane) must be amortised over several
+// cells per thread; four blocks of 256 threads per SM still keep enough loads
+// in flight for the HBM-bound solves.
 static int nblocks(long long n) {
-  long long b = (n + kThreads - 1) / kThreads;
-  return (int)std::max(1LL, std::min<long long>(b, kMaxBlocks));
+  const int sm = std::max(1, device_info().sm_count);
+  const long long cpt = std::max(1, g_cfd_cells_per_thread);
+  const long long cap = std::min<long long>((16 / cpt + 1) * (long long)sm, kMaxBlocks);
+  const long long b = (n + cpt * kThreads - 1) / (cpt * kThreads);
+  return (int)std::max(1LL, std::min(b, cap));
 }
 
 #define GRID_LOOP(c, n) \
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < (n); \
        c += (long long)gridDim.x * blockDim.x)
+
+// Post this block's partial of slot `slot`; true in the one block that
+// arrives last (it may then read every partial of the slot).
+__device__ bool post_partial(double v, double* P, int slot, unsigned* cnt, double* sh) {
+  __shared__ bool last;
+  const double t = block_allsum(v, sh);
+  if (threadIdx.x == 0) {
+    P[slot * kMaxBlocks + blockIdx.x] = t;
+    __threadfence();
+    last = atomicAdd(&cnt[slot], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+// Two sums posted together under the counter of slot `s1`.
+__device__ bool post_pair(double v1, double v2, double* P, int s1, int s2, unsigned* cnt,
+                          double* sh) {
+  __shared__ bool last;
+  const double a1 = block_allsum(v1, sh);
+  const double a2 = block_allsum(v2, sh);
+  if (threadIdx.x == 0) {
+    P[s1 * kMaxBlocks + blockIdx.x] = a1;
+    P[s2 * kMaxBlocks + blockIdx.x] = a2;
+    __threadfence();
+    last = atomicAdd(&cnt[s1], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+// In the last block: the slot's partials added in block order; resets the
+// slot's counter (a slot read through another slot's counter leaves its own
+// counter at zero, where it already is).
+__device__ double total(const double* P, int slot, unsigned* cnt, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+    v += __ldcg(P + slot * kMaxBlocks + i);
+  const double r = block_allsum(v, sh);
+  if (threadIdx.x == 0) cnt[slot] = 0u;
+  return r;
+}
 
 __device__ __forceinline__ double apply_row(const Dims& d, const double* vals, const double* u,
                                             long long c) {
@@ -178,8 +241,10 @@ __device__ __forceinline__ double apply_row(const Dims& d, const double* vals, c
   return acc;
 }
 
+// x = 0, r = rhat = p = q = b; the last block sets up the scalars
 __global__ void k_setup(long long n, const double* b, double* x, double* r, double* rhat,
-                        double* p, double* q, double* P) {
+                        double* p, double* q, double* P, KState* st, double tol, double atol,
+                        long long maxiter) {
   __shared__ double sh[33];
   double bb = 0.0;
   GRID_LOOP(c, n) {
@@ -191,40 +256,36 @@ __global__ void k_setup(long long n, const double* b, double* x, double* r, doub
     q[c] = v;
     bb += v * v;
   }
-  put_partial(bb, P + P_BB * kMaxBlocks, sh);
-}
-
-__global__ void k_init(KState* st, const double* P, int nb, double tol, double atol,
-                       long long maxiter) {
-  __shared__ double sh[33];
-  const double bs = sum_partials(P + P_BB * kMaxBlocks, nb, sh);
+  if (!post_partial(bb, P, P_BB, st->cnt, sh)) return;
+  const double bs = total(P, P_BB, st->cnt, sh);
   if (threadIdx.x == 0) {
     const double a2 = tol * tol * bs, b2 = atol * atol;
     st->atol2 = a2 > b2 ? a2 : b2;
     st->rho = st->alpha = st->omega = 1.0;
     st->rho_new = bs;  // <rhat, r> with rhat = r = b
     st->rs = bs;
+    st->bb = bs;
     st->k = 0;
     st->maxiter = maxiter;
     st->done = !(bs > st->atol2 && 0 < maxiter);
   }
 }
 
-// p = r + beta (p - omega q); phat = M p
+// p = r + beta (p - omega q); phat = M p (dinv: the Jacobi reciprocals, or NULL)
 __global__ void k_a(long long n, const KState* st, const double* r, double* p, const double* q,
-                    double* phat, const double* diag) {
+                    double* phat, const double* dinv) {
   if (st->done) return;
   const double beta = st->rho_new / st->rho * st->alpha / st->omega;
   const double om = st->omega;
   GRID_LOOP(c, n) {
     const double v = r[c] + beta * (p[c] - om * q[c]);
     p[c] = v;
-    phat[c] = diag ? v / diag[c] : v;
+    phat[c] = dinv ? dinv[c] * v : v;
   }
 }
 
-// q = A phat; partial <rhat, q>
-__global__ void k_b(Dims d, const KState* st, const double* vals, const double* phat, double* q,
+// q = A phat; alpha = rho / <rhat, q>
+__global__ void k_b(Dims d, KState* st, const double* vals, const double* phat, double* q,
                     const double* rhat, double* P) {
   if (st->done) return;
   __shared__ double sh[33];
@@ -234,27 +295,31 @@ __global__ void k_b(Dims d, const KState* st, const double* vals, const double* 
     q[c] = v;
     acc += rhat[c] * v;
   }
-  put_partial(acc, P + P_RQ * kMaxBlocks, sh);
+  if (!post_partial(acc, P, P_RQ, st->cnt, sh)) return;
+  const double rq = total(P, P_RQ, st->cnt, sh);
+  if (threadIdx.x == 0) st->alpha_cur = st->rho_new / rq;
 }
 
-// alpha = rho / <rhat, q>; s = r - alpha q; shat = M s; partial <s, s>
-__global__ void k_c(long long n, const KState* st, const double* P, int nb, const double* r,
-                    const double* q, double* s, double* shat, const double* diag, double* Pout) {
+// s = r - alpha q; shat = M s; <s, s>
+__global__ void k_c(long long n, KState* st, const double* r, const double* q, double* s,
+                    double* shat, const double* dinv, double* P) {
   if (st->done) return;
   __shared__ double sh[33];
-  const double alpha = st->rho_new / sum_partials(P + P_RQ * kMaxBlocks, nb, sh);
+  const double alpha = st->alpha_cur;
   double acc = 0.0;
   GRID_LOOP(c, n) {
     const double v = r[c] - alpha * q[c];
     s[c] = v;
-    shat[c] = diag ? v / diag[c] : v;
+    shat[c] = dinv ? dinv[c] * v : v;
     acc += v * v;
   }
-  put_partial(acc, Pout + P_SS * kMaxBlocks, sh);
+  if (!post_partial(acc, P, P_SS, st->cnt, sh)) return;
+  const double ss = total(P, P_SS, st->cnt, sh);
+  if (threadIdx.x == 0) st->ss = ss;
 }
 
-// t = A shat; partials <t, s>, <t, t>
-__global__ void k_d(Dims d, const KState* st, const double* vals, const double* shat, double* t,
+// t = A shat; omega = <t, s> / <t, t>
+__global__ void k_d(Dims d, KState* st, const double* vals, const double* shat, double* t,
                     const double* s, double* P) {
   if (st->done) return;
   __shared__ double sh[33];
@@ -265,21 +330,20 @@ __global__ void k_d(Dims d, const KState* st, const double* vals, const double* 
     ts += v * s[c];
     tt += v * v;
   }
-  put_partial(ts, P + P_TS * kMaxBlocks, sh);
-  put_partial(tt, P + P_TT * kMaxBlocks, sh);
+  if (!post_pair(ts, tt, P, P_TS, P_TT, st->cnt, sh)) return;
+  const double tsv = total(P, P_TS, st->cnt, sh);
+  const double ttv = total(P, P_TT, st->cnt, sh);
+  if (threadIdx.x == 0) st->omega_cur = tsv / ttv;
 }
 
-// x, r update (early exit when <s, s> < atol2); partials <r, r>, <rhat, r>
-__global__ void k_e(long long n, const KState* st, double* P, int nb, double* x, double* r,
-                    const double* s, const double* t, const double* phat, const double* shat,
-                    const double* rhat) {
+// x, r update (early exit when <s, s> < atol2); <r, r>, <rhat, r>; the
+// scalar step of the iteration (JAX's k, breakdown codes and stop test)
+__global__ void k_e(long long n, KState* st, double* P, double* x, double* r, const double* s,
+                    const double* t, const double* phat, const double* shat, const double* rhat) {
   if (st->done) return;
   __shared__ double sh[33];
-  const double alpha = st->rho_new / sum_partials(P + P_RQ * kMaxBlocks, nb, sh);
-  const bool exit_early = sum_partials(P + P_SS * kMaxBlocks, nb, sh) < st->atol2;
-  const double ts = sum_partials(P + P_TS * kMaxBlocks, nb, sh);
-  const double tt = sum_partials(P + P_TT * kMaxBlocks, nb, sh);
-  const double omega = ts / tt;
+  const double alpha = st->alpha_cur, omega = st->omega_cur;
+  const bool exit_early = st->ss < st->atol2;
   double rr = 0.0, rhr = 0.0;
   GRID_LOOP(c, n) {
     double rn;
@@ -294,28 +358,17 @@ __global__ void k_e(long long n, const KState* st, double* P, int nb, double* x,
     rr += rn * rn;
     rhr += rhat[c] * rn;
   }
-  put_partial(rr, P + P_RR * kMaxBlocks, sh);
-  put_partial(rhr, P + P_RHR * kMaxBlocks, sh);
-}
-
-// scalar step (one block)
-__global__ void k_s(KState* st, const double* P, int nb) {
-  if (st->done) return;
-  __shared__ double sh[33];
-  const double rho_ = st->rho_new;
-  const double alpha = rho_ / sum_partials(P + P_RQ * kMaxBlocks, nb, sh);
-  const double ts = sum_partials(P + P_TS * kMaxBlocks, nb, sh);
-  const double tt = sum_partials(P + P_TT * kMaxBlocks, nb, sh);
-  const double omega = ts / tt;
-  const double rs = sum_partials(P + P_RR * kMaxBlocks, nb, sh);
-  const double rhr = sum_partials(P + P_RHR * kMaxBlocks, nb, sh);
+  if (!post_pair(rr, rhr, P, P_RR, P_RHR, st->cnt, sh)) return;
+  const double rs = total(P, P_RR, st->cnt, sh);
+  const double rh = total(P, P_RHR, st->cnt, sh);
   if (threadIdx.x == 0) {
+    const double rho_ = st->rho_new;
     long long k = (omega == 0.0 || alpha == 0.0) ? -11 : st->k + 1;
     if (rho_ == 0.0) k = -10;
     st->rho = rho_;
     st->alpha = alpha;
     st->omega = omega;
-    st->rho_new = rhr;
+    st->rho_new = rh;
     st->rs = rs;
     st->k = k;
     st->done = !(rs > st->atol2 && k < st->maxiter && k >= 0);
@@ -328,36 +381,113 @@ static cudaError_t read_state(const KState* dst, KState* host, cudaStream_t s) {
   return cudaStreamSynchronize(s);
 }
 
-// Solve vals x = b (diag: Jacobi preconditioner or NULL); *iters = JAX's k.
-static int krylov(const Dims& d, const double* vals, const double* diag, const double* b,
+// One chunk of kChunk iterations, launched directly ...
+constexpr int kChunk = 8;
+static void launch_chunk(const Dims& d, const double* vals, const double* dinv, double* x,
+                         const Work& w, int nb, cudaStream_t s) {
+  const long long n = d.n;
+  for (int it = 0; it < kChunk; ++it) {
+    k_a<<<nb, kThreads, 0, s>>>(n, w.st, w.r, w.p, w.q, w.phat, dinv);
+    k_b<<<nb, kThreads, 0, s>>>(d, w.st, vals, w.phat, w.q, w.rhat, w.P);
+    k_c<<<nb, kThreads, 0, s>>>(n, w.st, w.r, w.q, w.s, w.shat, dinv, w.P);
+    k_d<<<nb, kThreads, 0, s>>>(d, w.st, vals, w.shat, w.t, w.s, w.P);
+    k_e<<<nb, kThreads, 0, s>>>(n, w.st, w.P, x, w.r, w.s, w.t, w.phat, w.shat, w.rhat);
+  }
+}
+
+// ... or as a CUDA graph captured once per argument set (operator, reciprocals,
+// solution and scratch buffers, grid) and replayed.  The cache only grows: an
+// executable is never destroyed, so one in flight on another thread stays
+// valid; past kMaxGraphs argument sets the chunks are launched directly.
+struct GraphKey {
+  const void *vals, *dinv, *x, *r, *P;  // r and P fix the scratch layout
+  long long n;
+  int nx, ny, nz, dev, nb;
+  bool operator==(const GraphKey& o) const {
+    return vals == o.vals && dinv == o.dinv && x == o.x && r == o.r && P == o.P && n == o.n &&
+           nx == o.nx && ny == o.ny && nz == o.nz && dev == o.dev && nb == o.nb;
+  }
+};
+constexpr int kMaxGraphs = 64;
+static std::mutex g_graph_mu;
+static GraphKey g_graph_keys[kMaxGraphs];
+static cudaGraphExec_t g_graph_execs[kMaxGraphs];
+static int g_graph_count = 0;
+
+static cudaGraphExec_t chunk_graph(const Dims& d, const double* vals, const double* dinv,
+                                   double* x, const Work& w, int nb) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  const GraphKey key{vals, dinv, x, w.r, w.P, d.n, d.nx, d.ny, d.nz, dev, nb};
+  std::lock_guard<std::mutex> lock(g_graph_mu);
+  for (int i = 0; i < g_graph_count; ++i)
+    if (g_graph_keys[i] == key) return g_graph_execs[i];
+  if (g_graph_count == kMaxGraphs) return nullptr;
+  cudaStream_t cap = nullptr;
+  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    launch_chunk(d, vals, dinv, x, w, nb, cap);
+    if (cudaStreamEndCapture(cap, &g) == cudaSuccess && g) {
+      if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) exec = nullptr;
+      cudaGraphDestroy(g);
+    }
+  }
+  cudaStreamDestroy(cap);
+  cudaGetLastError();  // a failed capture falls back to direct launches
+  if (!exec) return nullptr;
+  g_graph_keys[g_graph_count] = key;
+  g_graph_execs[g_graph_count] = exec;
+  ++g_graph_count;
+  return exec;
+}
+
+// Solve vals x = b (dinv: Jacobi reciprocals or NULL); *iters = JAX's k.
+static int krylov(const Dims& d, const double* vals, const double* dinv, const double* b,
                   double* x, double tol, double atol, long long maxiter, Work& w,
                   cudaStream_t s, long long* iters) {
   const long long n = d.n;
   const int nb = nblocks(n);
-  k_setup<<<nb, kThreads, 0, s>>>(n, b, x, w.r, w.rhat, w.p, w.q, w.P);
-  k_init<<<1, kThreads, 0, s>>>(w.st, w.P, nb, tol, atol, maxiter);
-  cudaError_t e = cudaGetLastError();
+  // the scalars and the last-block counters start from zero in every solve
+  cudaError_t e = cudaMemsetAsync(w.st, 0, sizeof(KState), s);
+  if (e != cudaSuccess) return record_cuda(e);
+  k_setup<<<nb, kThreads, 0, s>>>(n, b, x, w.r, w.rhat, w.p, w.q, w.P, w.st, tol, atol, maxiter);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return record_cuda(e);
   KState h{};
   e = read_state(w.st, &h, s);
   if (e != cudaSuccess) return record_cuda(e);
-  long long launched = 0, chunk = 4;
-  // at most maxiter iterations run; the stop flag is set no later than that
+  if (h.done) {
+    *iters = h.k;
+    return PFG_OK;
+  }
+  cudaGraphExec_t exec = chunk_graph(d, vals, dinv, x, w, nb);
+  long long launched = 0;
+  int reps = 1;
+  // at most maxiter iterations run; the stop flag is set no later than that;
+  // chunks launched after the stop return at once
   while (!h.done && launched < maxiter + 1) {
-    for (long long it = 0; it < chunk; ++it) {
-      k_a<<<nb, kThreads, 0, s>>>(n, w.st, w.r, w.p, w.q, w.phat, diag);
-      k_b<<<nb, kThreads, 0, s>>>(d, w.st, vals, w.phat, w.q, w.rhat, w.P);
-      k_c<<<nb, kThreads, 0, s>>>(n, w.st, w.P, nb, w.r, w.q, w.s, w.shat, diag, w.P);
-      k_d<<<nb, kThreads, 0, s>>>(d, w.st, vals, w.shat, w.t, w.s, w.P);
-      k_e<<<nb, kThreads, 0, s>>>(n, w.st, w.P, nb, x, w.r, w.s, w.t, w.phat, w.shat, w.rhat);
-      k_s<<<1, kThreads, 0, s>>>(w.st, w.P, nb);
+    for (int r = 0; r < reps; ++r) {
+      if (exec) {
+        e = cudaGraphLaunch(exec, s);
+        if (e != cudaSuccess) return record_cuda(e);
+      } else {
+        launch_chunk(d, vals, dinv, x, w, nb, s);
+      }
     }
-    launched += chunk;
+    launched += (long long)reps * kChunk;
     e = cudaGetLastError();
     if (e != cudaSuccess) return record_cuda(e);
     e = read_state(w.st, &h, s);
     if (e != cudaSuccess) return record_cuda(e);
-    chunk = std::min(chunk * 2, 64LL);
+    reps = std::min(reps * 2, 8);
   }
   *iters = h.k;
   return PFG_OK;
@@ -450,7 +580,7 @@ __global__ void k_energy_jacobian(Dims d, EnergyK K, const double* U, const doub
     }
     v0 += e.rho * cp_eff(e, T0[c]) / e.dt * d.dV;
     vals[c] = v0;
-    diag[c] = v0 + dg;
+    diag[c] = 1.0 / (v0 + dg);  // the reference applies M as 1./precond_values * U
   }
 }
 
@@ -522,7 +652,7 @@ __global__ void k_momentum(Dims d, FlowK F, int comp, const double* T, const dou
     }
     v0 += (f.rho / f.dt + darcy) * d.dV;
     vals[c] = v0;
-    diag[c] = v0 + dg;
+    diag[c] = 1.0 / (v0 + dg);
   }
 }
 
@@ -659,6 +789,7 @@ static long long cells(const pfg_cfd_grid* g) { return (long long)g->nx * g->ny 
 static int check_grid(const pfg_cfd_grid* g) {
   if (!g) return PFG_ERR_NULL;
   if (g->nx < 1 || g->ny < 1 || g->nz < 1) return PFG_ERR_SHAPE;
+  if ((long long)g->nx * g->ny * g->nz >= (1LL << 31)) return PFG_ERR_SHAPE;  // 32-bit cell math
   if (!(g->dx > 0.0) || !(g->dy > 0.0) || !(g->dz > 0.0)) return PFG_ERR_PARAM;
   if (!(g->lx > 0.0) || !(g->ly > 0.0) || !(g->lz > 0.0)) return PFG_ERR_PARAM;
   return PFG_OK;
@@ -726,7 +857,9 @@ extern "C" int pfg_cfd_energy_solve(const pfg_cfd_grid* g, const pfg_cfd_energy*
   K.Ly = g->ly;
   K.Lz = g->lz;
   const int nb = nblocks(n);
-  double* norm = reinterpret_cast<double*>(w.st) + 16;  // after KState (< 128 bytes)
+  // the Newton residual norm^2 sits after the solver state, inside the 256-byte reserve
+  static_assert(sizeof(KState) <= 192, "solver state outgrew its reserve");
+  double* norm = reinterpret_cast<double*>(w.st) + 24;
   k_copy<<<nb, kThreads, 0, s>>>(n, T0, T_out);
   k_energy_residual<<<nb, kThreads, 0, s>>>(d, K, T_out, T0, conv_T, w.b, w.P);
   k_norm<<<1, kThreads, 0, s>>>(w.P, nb, norm);

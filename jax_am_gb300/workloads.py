@@ -14,6 +14,10 @@ so every polycrystal here is generated; see ``phase_field.utils.Field``).
   arrivals at 50 jobs/s, Nx, Ny ~ U[32, 160], Nz ~ U[16, 64],
   num_oris ~ U[10, 30], grains = cells / 2000, steps ~ U[100, 2000],
   gradient ~ U[5e5, 2e6] K/m.
+* ``cfd_simple_case``: the implicit CFD solver on the reference's standalone
+  CFD driver (``applications/cfd/simple/example.py:22-41`` and its
+  ``cfd_params.json``): 464 x 93 x 46 cells over 1 x 0.2 x 0.1 mm, a
+  348 x 46 x 18 local flow box, a 100 W surface Gaussian at 0.5 m/s.
 """
 import numpy as np
 
@@ -86,3 +90,18 @@ def differentiable_run(steps=500, checkpoint_every=25, seed=3):
     prob = LaserTrackProblem(pf_args, poly, g, w, dt, steps, x_start=20e-6, y=64e-6,
                              checkpoint_every=checkpoint_every)
     return prob, 200.0, 0.8
+
+
+def cfd_simple_case():
+    """``args`` for ``jax_am_gb300.cfd.cfd_am.AM_3d`` (meshes included)."""
+    from .cfd import cfd_am as G
+    dom, N = [1e-3, 2e-4, 1e-4], [464, 93, 46]
+    NL = [round(0.75 * N[0]), round(0.5 * N[1]), round(0.4 * N[2])]
+    args = dict(rho=8440.0, visco=7e-3, Marangoni=-2e-5, dt=1e-6, t_OFF=0.0012, speed=0.5,
+                X0=[2e-4, 1e-4, 1e-4], rb=5e-5, eta=0.43, P=100.0, T_ref=300.0, Ts=1563.0,
+                Tl=1623.0, latent_heat=270000.0, heat_source=0,
+                cp=G.LinearClip(0.2441, 338.39, 300.0, 1563.0),
+                k=G.LinearClip(0.0163105, 4.5847, 300.0, 1563.0))
+    args["mesh"] = G.mesh3d(dom, N)
+    args["mesh_local"] = G.mesh3d([0.75 * dom[0], 0.5 * dom[1], 0.4 * dom[2]], NL)
+    return args

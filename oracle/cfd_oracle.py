@@ -237,7 +237,8 @@ def solve_energy(mesh, args, T0, conv, Q, q_top, tol=1e-5, max_it=50):
         diag = jacobi_diag(vals)
         shape = U.shape
         A = lambda v: apply_op(vals, v.reshape(shape)).ravel()  # noqa: E731
-        M = lambda v: v / diag.ravel()  # noqa: E731
+        inv = 1.0 / diag.ravel()  # jacobiPreconditioner: 1./precond_values * U
+        M = lambda v: inv * v  # noqa: E731
         inc, kk = bicgstab(A, b.ravel(), M)
         lin.append(kk)
         U = U + inc.reshape(shape)
@@ -380,7 +381,7 @@ def solve_velocity(mesh_l, args, vel0, conv0, grad_p0, fl, T):
                                   grad_p0[..., comp], fl, comp, mg)
         diag = jacobi_diag(vals)
         A = lambda v, vals=vals: apply_op(vals, v.reshape(shape)).ravel()  # noqa: E731
-        M = lambda v, d=diag: v / d.ravel()  # noqa: E731
+        M = lambda v, inv=1.0 / diag.ravel(): inv * v  # noqa: E731
         x, kk = bicgstab(A, b.ravel(), M, tol=1e-10, maxiter=10000)
         iters.append(kk)
         vel[..., comp] = x.reshape(shape)
