@@ -401,6 +401,23 @@ def profile_run(args):
                       "plan": _lib.describe_plan(solver.params)}), flush=True)
 
 
+def profile_cfd(args):
+    """``--steps`` eager steps of the CFD driver case (``time_cfd``'s
+    workload), each phase in an NVTX range (``AM_3d.energy``,
+    ``AM_3d.flow``): ``ncu --nvtx --nvtx-include "AM_3d.flow/" ...
+    python bench.py --profile-cfd --steps 3`` captures the third step's flow
+    solve (the first two have no flow yet)."""
+    import __graft_entry__
+    __graft_entry__.build()
+    from jax_am_gb300.cfd import cfd_am as G
+    from jax_am_gb300.workloads import cfd_simple_case
+    s = G.AM_3d(cfd_simple_case())
+    for _ in range(args.steps):
+        s.time_integration()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_cfd": True, "steps": args.steps, **s.iterations()}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -412,6 +429,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-cfd", action="store_true", help="skip the implicit CFD solver leg")
+    ap.add_argument("--profile-cfd", action="store_true",
+                    help="eager steps of the CFD driver case for ncu (see profile_cfd)")
     ap.add_argument("--cfd-cpu", action="store_true",
                     help="also time one step of the float64 CPU oracle of the CFD solver")
     ap.add_argument("--no-configs", action="store_true",
@@ -422,6 +441,9 @@ def main():
                     help="orientation count of the --profile workload")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.profile_cfd:
+        profile_cfd(args)
+        return
     if args.profile:
         profile_run(args)
         return

@@ -219,6 +219,8 @@ class AM_3d:
         s = _stream()
         e = self._energy_struct()
         T_new = torch.empty_like(self.T)
+        # NVTX ranges name the two phases for profilers (ncu --nvtx-include)
+        torch.cuda.nvtx.range_push("AM_3d.energy")
         st = lib.pfg_cfd_energy_solve(ctypes.byref(self._grid), ctypes.byref(e),
                                       _lib.ptr(self.T), _lib.ptr(self.conv_T), _lib.ptr(T_new),
                                       _lib.ptr(self._ws), self._ws.numel(),
@@ -228,6 +230,8 @@ class AM_3d:
         st = lib.pfg_cfd_solid_update(ctypes.byref(self._grid), float(a["Ts"]), float(a["Tl"]),
                                       _lib.ptr(self.T), _lib.ptr(self.solidID), s)
         _lib.check(st, "pfg_cfd_solid_update")
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.nvtx.range_push("AM_3d.flow")
         x0, _, y0, _, z0, _ = self.get_moving_box_boundary(self.t)
         f = _lib.CfdFlow()
         f.rho, f.visco, f.dt = float(a["rho"]), float(a["visco"]), float(a["dt"])
@@ -238,6 +242,7 @@ class AM_3d:
                                    _lib.ptr(self.conv), _lib.ptr(self.grad_p0),
                                    _lib.ptr(self.conv_T), _lib.ptr(self._ws), self._ws.numel(),
                                    ctypes.byref(self.stats), s)
+        torch.cuda.nvtx.range_pop()
         _lib.check(st, "pfg_cfd_flow_step")
         self.t += a["dt"]
 

@@ -121,3 +121,59 @@ def test_coupling_transpose_and_outputs(tmp_path):
     with pytest.raises(ValueError):
         s.inspect_sol(1, 1)
     assert os.path.exists(path)
+
+
+def test_coupled_driver_loop_vs_oracles():
+    """The coupled driver's loop (applications/phase_field/coupled/
+    example.py:86-111): the CFD solver every 1e-6 s, the phase field every
+    2e-7 s on the same 12 x 8 x 5 grid, fed r T_past + (1 - r) T_future
+    through InterpolatedT.  The same loop with the float64 CFD oracle and the
+    float64 phase-field oracle fed the same float32 interpolated fields gives
+    the reference: eta within 1e-4, argmax maps exact."""
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    from jax_am_gb300.phase_field.coupling import InterpolatedT, convert_temperature
+    from oracle import pf_oracle as O
+    from tests.cases import f32, pf_case
+    h = float(GOLD["h"])
+    N = [int(v) for v in GOLD["grid"]]
+    NL = [int(v) for v in GOLD["local"]]
+    cfd = gpu_solver(CASES["surface"], N, NL, h, tuple(GOLD["cp"]), tuple(GOLD["k"]))
+    ocfd = oracle_solver(CASES["surface"], N, NL, h, tuple(GOLD["cp"]), tuple(GOLD["k"]))
+    poly, eta, _, pf_args, oargs, _ = pf_case(tuple(N), 6, 0.15, seed=11, h=(h, h, h), noise=0.3)
+    pf = PFSolver(pf_args, poly)
+    dt_pf, dt_cfd = 2e-7, float(CASES["surface"]["dt"])
+    pf_ts = np.arange(0.0, 3e-6 + 1e-10, dt_pf)
+
+    def fields():
+        return (cfd.T[:, :, :, 0].clone(), np.float32(ocfd.T))
+
+    T_past, oT_past = fields()
+    cfd.time_integration()
+    ocfd.time_integration()
+    T_future, oT_future = fields()
+    t_cfd = dt_cfd
+    state = (torch.tensor(eta, dtype=torch.float32, device="cuda"), float(pf_ts[0]))
+    e_ref = eta.astype(np.float64)
+    hot = 0
+    for t_pf in pf_ts[1:]:
+        if t_pf > t_cfd + dt_cfd:
+            cfd.time_integration()
+            ocfd.time_integration()
+            T_past, oT_past = T_future, oT_future
+            T_future, oT_future = fields()
+            t_cfd += dt_cfd
+        src = InterpolatedT(convert_temperature(T_past), convert_temperature(T_future), t_cfd,
+                            dt_cfd)
+        t_prev = state[1]
+        state, _ = pf.stepper(state, float(t_pf), [src])
+        r = np.float32((t_cfd - t_pf) / dt_cfd)
+        Tmix = r * oT_past + (np.float32(1.0) - r) * oT_future
+        T_cells = f32(np.transpose(Tmix, (2, 1, 0)).reshape(-1, 1))
+        hot = max(hot, int((T_cells > 1623.0).sum()))
+        e_ref = O.explicit_euler(e_ref, t_prev, float(t_pf), T_cells, oargs,
+                                 poly.unique_grain_directions)
+    got = state[0].double().cpu().numpy()
+    err = float(np.abs(got - e_ref).max())
+    mism = int(np.sum(np.argmax(got, axis=1) != np.argmax(e_ref, axis=1)))
+    assert hot > 0, "the coupled case must melt"
+    assert err <= 1e-4 and mism == 0, (err, mism)
