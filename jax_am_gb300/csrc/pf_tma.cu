@@ -123,18 +123,38 @@ __device__ __forceinline__ float4 tma_fold(const PFConsts& c, const TempCoef& tc
 // bulk copy starts on a 16-byte boundary and moves a multiple of 16 bytes
 // without leaving the grid row, and the tile's first cell sits at position
 // x0 - base of the staged row.
-template <bool ANISO, int TSRC, int NC, int VEC>
+// The launch plan of the common large-grid case with 20 orientations (every
+// configuration of the reference uses num_oris = 20): 24 x 10 cell tiles,
+// 6 cells x 5 lanes per warp row, 5 rows per warp, 4 ring slots.  With
+// FIX = 1 the kernel takes these as compile-time constants (the host launches
+// it only for exactly this plan), which folds the tile arithmetic into
+// immediate offsets.
+struct FixedPlan20 {
+  static constexpr int n = 20, tx = 24, ty = 10, rpw = 5, cpw = 6, wx = 4, tpc = 5, stages = 4;
+  static constexpr int pitch = (tx + 2) * n, tslot = ((ty + 2) * (tx + 2) + 3) / 4 * 4;
+};
+
+template <bool ANISO, int TSRC, int NC, int VEC, int FIX>
 __global__ void __launch_bounds__(NC, NC == 256 ? 2 : 1)
 pf_tma_kernel(const __grid_constant__ StepArgs a) {
   static_assert(VEC == 4 || VEC == 2, "16- or 8-byte vectors");
+  static_assert(FIX == 0 || (VEC == 4 && NC == 256), "the fixed plan is a 16-byte, 256-thread plan");
+  using FP = FixedPlan20;
+  constexpr bool kFix = FIX == 1;
+  // tile plan: compile-time constants under FIX, the launch arguments otherwise
+  const int P_n = kFix ? FP::n : a.n, P_pitch = kFix ? FP::pitch : a.pitch;
+  const int P_tx = kFix ? FP::tx : a.tx, P_ty = kFix ? FP::ty : a.ty;
+  const int P_rpw = kFix ? FP::rpw : a.rpw, P_cpw = kFix ? FP::cpw : a.cpw;
+  const int P_wx = kFix ? FP::wx : a.wx, P_tpc = kFix ? FP::tpc : a.tpc;
+  const int P_stages = kFix ? FP::stages : a.stages, P_tslot = kFix ? FP::tslot : a.tslot;
   constexpr int kTQ = 3;  // temperature cells staged per thread and plane, at most
   extern __shared__ __align__(128) float smem[];
-  const int S = a.stages;
-  const int slot_floats = (a.ty + 2) * a.pitch;
+  const int S = P_stages;
+  const int slot_floats = (P_ty + 2) * P_pitch;
   float* eta_s = smem;
   float* T_s = eta_s + (size_t)S * slot_floats;
-  float4* cc = reinterpret_cast<float4*>(T_s + (size_t)S * a.tslot);  // [2][ty * tx]
-  uint64_t* full = reinterpret_cast<uint64_t*>(cc + 2 * a.ty * a.tx);
+  float4* cc = reinterpret_cast<float4*>(T_s + (size_t)S * P_tslot);  // [2][ty * tx]
+  uint64_t* full = reinterpret_cast<uint64_t*>(cc + 2 * P_ty * P_tx);
 
   // ---- work unit
   const int per_plane = a.tiles_x * a.tiles_y;
@@ -142,11 +162,11 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   const int rem = blockIdx.x - zi * per_plane;
   const int byi = rem / a.tiles_x;
   const int bxi = rem - byi * a.tiles_x;
-  const int x0 = bxi * a.tx, y0 = byi * a.ty;
-  const int xe = min(x0 + a.tx, a.nx), ye = min(y0 + a.ty, a.ny);
+  const int x0 = bxi * P_tx, y0 = byi * P_ty;
+  const int xe = min(x0 + P_tx, a.nx), ye = min(y0 + P_ty, a.ny);
   const int zb = zi * a.zc, ze = min(zb + a.zc, a.nz);
   const int txv = xe - x0, tyv = ye - y0;
-  const int n = a.n;
+  const int n = P_n;
   const int nplanes = ze - zb + 2;  // planes zb-1 .. ze
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -204,7 +224,7 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   const unsigned cell_bytes = (unsigned)(n * 4);
   const unsigned plane_bytes =
       (unsigned)rows * (row_bytes + (wrap_left ? cell_bytes : 0u) + (wrap_right ? cell_bytes : 0u));
-  const int tp = a.tx + 2;
+  const int tp = P_tx + 2;
   const int gsy = a.nx + 2, gsz = (a.ny + 2) * (a.nx + 2);  // ghosted strides (host checks < 2^31)
   // this thread's temperature cells of a plane: offsets fixed for the unit
   int t_src[kTQ], t_dst[kTQ];
@@ -236,13 +256,13 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
       for (int r = lane; r < rows; r += 32) {
         const int gy = bc_index(y0 - 1 + r, a.ny, a.bcy);
         const float* src_row = a.eta_in + ((int64_t)gz * a.ny + gy) * a.nx * n;
-        float* dst_row = es + r * a.pitch;
+        float* dst_row = es + r * P_pitch;
         tma_row(dst_row + dst_cell0 * n, src_row + (int64_t)cx0 * n, row_bytes, &full[s]);
         if (wrap_left) tma_row(dst_row, src_row + (int64_t)(a.nx - 1) * n, cell_bytes, &full[s]);
         if (wrap_right) tma_row(dst_row + (txv + 1) * n, src_row, cell_bytes, &full[s]);
       }
     }
-    float* ts = T_s + (size_t)s * a.tslot;
+    float* ts = T_s + (size_t)s * P_tslot;
     if constexpr (TSRC == kTHeat) {
       const float* tplane = a.T + (int64_t)(pz + 1) * gsz;
 #pragma unroll
@@ -260,11 +280,11 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   };
 
   // ---- lane -> (cell, orientation chunk)
-  const int tpc = a.tpc;
-  const int wxi = warp % a.wx, wyi = warp / a.wx;
+  const int tpc = P_tpc;
+  const int wxi = warp % P_wx, wyi = warp / P_wx;
   const int lc = lane / tpc, kk = lane - lc * tpc;
-  const bool lane_active = lc < a.cpw;
-  const int xs = wxi * a.cpw + (lane_active ? lc : 0);
+  const bool lane_active = lc < P_cpw;
+  const int xs = wxi * P_cpw + (lane_active ? lc : 0);
   const bool col_valid = lane_active && xs < txv;
   const int xsp = xs + pos0;  // staged-row position of this lane's cell
   const int i0 = kk * VEC;
@@ -302,9 +322,9 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     const int i = threadIdx.x + q * NC;
     c_ok[q] = i < ncell;
     const int r = c_ok[q] ? i / txv : 0, c = c_ok[q] ? i - r * txv : 0;
-    c_eoff[q] = (r + 1) * a.pitch + (c + pos0) * n;
+    c_eoff[q] = (r + 1) * P_pitch + (c + pos0) * n;
     c_toff[q] = (r + 1) * tp + c + 1;
-    c_cc[q] = r * a.tx + c;
+    c_cc[q] = r * P_tx + c;
     c_hx[q] = x0 + c;
     c_hy[q] = y0 + r;
     c_g[q] = (c_hy[q] + 1) * gsy + c_hx[q] + 1;
@@ -313,8 +333,8 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   // per-cell coefficients of plane pz (in slot s) -> cc[buf]
   auto cell_coefs = [&](int s, int buf, int pz) {
     const float* es = eta_s + (size_t)s * slot_floats;
-    const float* ts = T_s + (size_t)s * a.tslot;
-    float4* cb = cc + (size_t)buf * a.ty * a.tx;
+    const float* ts = T_s + (size_t)s * P_tslot;
+    float4* cb = cc + (size_t)buf * P_ty * P_tx;
     TempCoef plane{};
     if constexpr (TSRC == kTQuench) {
       const double zc = a.q.z_first + (double)pz * (double)a.h_z;
@@ -375,8 +395,8 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   const int64_t plane_elems = (int64_t)a.ny * a.nx * n;
   const int64_t row_elems = (int64_t)a.nx * n;
   const int64_t col_base = ((int64_t)y0 * a.nx + gx) * n + i0;
-  const int r_begin = wyi * a.rpw;
-  const int r_end = min(r_begin + a.rpw, tyv);
+  const int r_begin = wyi * P_rpw;
+  const int r_end = min(r_begin + P_rpw, tyv);
   // ring slots of planes m, m+1, m+2 and the phase parity of plane m+2,
   // rotated each iteration (plane j is in slot j % S)
   int s_prev = 0, s_cur = 1, s_next = 2;
@@ -394,9 +414,9 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     }
 
     if constexpr (TSRC == kTHeat) {
-      const float* tp_ = T_s + (size_t)s_prev * a.tslot;
-      const float* tc_ = T_s + (size_t)s_cur * a.tslot;
-      const float* tn_ = T_s + (size_t)s_next * a.tslot;
+      const float* tp_ = T_s + (size_t)s_prev * P_tslot;
+      const float* tc_ = T_s + (size_t)s_cur * P_tslot;
+      const float* tn_ = T_s + (size_t)s_next * P_tslot;
       const int zoff = (z + 1) * gsz;
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
@@ -414,12 +434,12 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     const float* e_cur = eta_s + (size_t)s_cur * slot_floats;
     const float* e_prev = eta_s + (size_t)s_prev * slot_floats;
     const float* e_next = eta_s + (size_t)s_next * slot_floats;
-    const float4* ccb = cc + (size_t)(m & 1) * a.ty * a.tx;
+    const float4* ccb = cc + (size_t)(m & 1) * P_ty * P_tx;
     float* out_row = a.eta_out + ((int64_t)z * plane_elems + col_base + (int64_t)r_begin * row_elems);
     auto row_out = [&](int r, float* dst, const VecF<VEC>& c, const VecF<VEC>& xm,
                        const VecF<VEC>& xp, const VecF<VEC>& ym, const VecF<VEC>& yp,
                        const VecF<VEC>& zm, const VecF<VEC>& zp) {
-      const float4 kc = ccb[r * a.tx + xs];
+      const float4 kc = ccb[r * P_tx + xs];
       VecF<VEC> out;
 #pragma unroll
       for (int v = 0; v < VEC; ++v)
@@ -430,13 +450,13 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     int r = r_begin;
     // two rows at a time: rows r-1 .. r+2 of the plane are loaded once
     for (; r + 1 < r_end; r += 2, out_row += 2 * row_elems) {
-      const int off = (r + 1) * a.pitch + xsp * n + i0;
-      const int off2 = off + a.pitch;
+      const int off = (r + 1) * P_pitch + xsp * n + i0;
+      const int off2 = off + P_pitch;
       VecF<VEC> ym, c, c2, yp2, xm, xp, xm2, xp2, zm, zp, zm2, zp2;
-      ym.load(e_cur + off - a.pitch);
+      ym.load(e_cur + off - P_pitch);
       c.load(e_cur + off);
       c2.load(e_cur + off2);
-      yp2.load(e_cur + off2 + a.pitch);
+      yp2.load(e_cur + off2 + P_pitch);
       xm.load(e_cur + off + off_xm);
       xp.load(e_cur + off + off_xp);
       xm2.load(e_cur + off2 + off_xm);
@@ -449,13 +469,13 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
       row_out(r + 1, out_row + row_elems, c2, xm2, xp2, c, yp2, zm2, zp2);
     }
     if (r < r_end) {
-      const int off = (r + 1) * a.pitch + xsp * n + i0;
+      const int off = (r + 1) * P_pitch + xsp * n + i0;
       VecF<VEC> c, xm, xp, ym, yp, zm, zp;
       c.load(e_cur + off);
       xm.load(e_cur + off + off_xm);
       xp.load(e_cur + off + off_xp);
-      ym.load(e_cur + off - a.pitch);
-      yp.load(e_cur + off + a.pitch);
+      ym.load(e_cur + off - P_pitch);
+      yp.load(e_cur + off + P_pitch);
       zm.load(e_prev + off);
       zp.load(e_next + off);
       row_out(r, out_row, c, xm, xp, ym, yp, zm, zp);
@@ -506,9 +526,9 @@ bool plan_tma_tiles(int nx, int ny, int nz, int n, int bcx, int sm_count, int ma
   return true;
 }
 
-template <bool ANISO, int TSRC, int NC, int VEC>
+template <bool ANISO, int TSRC, int NC, int VEC, int FIX = 0>
 static cudaError_t launch_tma_t(const StepArgs& a, const TilePlan& t, cudaStream_t s) {
-  auto k = pf_tma_kernel<ANISO, TSRC, NC, VEC>;
+  auto k = pf_tma_kernel<ANISO, TSRC, NC, VEC, FIX>;
   static int configured[64] = {0};
   const int dev = device_info().device;
   if (dev < 0 || dev >= 64 || configured[dev] < (int)t.smem) {
@@ -521,8 +541,22 @@ static cudaError_t launch_tma_t(const StepArgs& a, const TilePlan& t, cudaStream
   return cudaGetLastError();
 }
 
+// the plan is exactly FixedPlan20
+static bool is_fixed_plan20(const StepArgs& a, const TilePlan& t) {
+  using FP = FixedPlan20;
+  return t.rs == 256 && t.vec == 4 && a.n == FP::n && t.tx == FP::tx && t.ty == FP::ty &&
+         t.rpw == FP::rpw && t.cpw == FP::cpw && t.wx == FP::wx && t.tpc == FP::tpc &&
+         t.stages == FP::stages && t.pitch == FP::pitch && t.tslot == FP::tslot &&
+         a.pitch == FP::pitch && a.tx == FP::tx && a.ty == FP::ty && a.rpw == FP::rpw &&
+         a.cpw == FP::cpw && a.wx == FP::wx && a.tpc == FP::tpc && a.stages == FP::stages &&
+         a.tslot == FP::tslot;
+}
+
 template <int TSRC>
 cudaError_t launch_tma_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s) {
+  if (is_fixed_plan20(a, t))
+    return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 256, 4, 1>(a, t, s)
+                              : launch_tma_t<false, TSRC, 256, 4, 1>(a, t, s);
   if (t.rs == 512)
     return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 512, 4>(a, t, s)
                               : launch_tma_t<false, TSRC, 512, 4>(a, t, s);

@@ -145,3 +145,57 @@ def test_multi_track_laser_reduced():
     path = raster([10e-6, 20e-6, 30e-6], 1.0, 250.0, 20e-6, 21e-6)
     _laser_case((80, 40, 20), 30, 40, 0.15, path, 150, 5,
                 "multi track 80x40x20 n=30 A=0.15, 150 steps")
+
+
+def _assert_fixed_plan(pf_args, poly):
+    """The step kernel takes the compile-time 24 x 10 plan (FixedPlan20 in
+    pf_tma.cu) exactly when the planner picks this plan."""
+    from jax_am_gb300 import _lib
+    from jax_am_gb300.phase_field.allen_cahn import make_pf_params
+    p = _lib.describe_plan(make_pf_params(pf_args, poly))
+    got = (p["kernel"], p["vec"], p["tile_x"], p["tile_y"], p["rows_per_warp"], p["warps_x"],
+           p["slots"])
+    assert got == (3, 4, 24, 10, 5, 4, 4), p
+
+
+def test_fixed_plan_fused_laser_vs_oracle():
+    """200 x 100 x 50 cells with n = 20 (partial tiles along x, as the bench
+    grid): the bench kernel's compile-time plan, 40 fused heat + anisotropic
+    steps against the float64 oracle."""
+    from jax_am_gb300.phase_field.utils import Field
+    from jax_am_gb300.runner import single_track
+    pf_args = dict(PF_KEYS, Nx=200, Ny=100, Nz=50, h=1e-6, num_grains=300, num_oris=20,
+                   T_liquidus=1623.0, anisotropy=0.15)
+    _assert_fixed_plan(pf_args, Field(pf_args, seed=5))
+    path = single_track(20e-6, 50e-6, 0.8, 200.0, 1.0)
+    Tmax = _laser_case((200, 100, 50), 20, 300, 0.15, path, 40, 5,
+                       "fixed 24x10 plan, 200x100x50 n=20 A=0.15, 40 fused steps")
+    assert Tmax > 300.0
+
+
+@pytest.mark.parametrize("aniso", [0.0, 0.15])
+def test_fixed_plan_T_array_vs_oracle(aniso):
+    """120 x 100 x 40 cells, n = 20, a temperature array (the drivers'
+    stepper form): the compile-time plan against float64, three steps."""
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    from jax_am_gb300.phase_field.utils import Field
+    nx, ny, nz = 120, 100, 40
+    pf_args = dict(PF_KEYS, Nx=nx, Ny=ny, Nz=nz, h=1e-6, num_grains=200, num_oris=20,
+                   T_liquidus=1623.0, anisotropy=aniso)
+    poly = Field(pf_args, seed=6)
+    _assert_fixed_plan(pf_args, poly)
+    s = PFSolver(pf_args, poly)
+    g = torch.Generator(device="cuda").manual_seed(7)
+    e0 = s.ini_cond()
+    e0 = torch.clamp(e0 + 0.3 * torch.rand(e0.shape, generator=g, device="cuda"), 0.0, 1.0)
+    T = 1450.0 + 300.0 * torch.rand((s.N, 1), generator=g, device="cuda")
+    dt = float(np.float32(1e-8))
+    state = (e0.clone(), 0.0)
+    for k in range(3):
+        state, _ = s.stepper(state, (k + 1) * dt, [T])
+    a = _oracle_args(pf_args, poly)
+    e = e0.double().reshape(nz, ny, nx, -1)
+    T3 = T.double().reshape(nz, ny, nx)
+    for _ in range(3):
+        e = e + dt * PT.pf_increment(e, T3, a, _dirs(poly))
+    _compare(f"fixed 24x10 plan, T array, A={aniso}", state[0], e)
