@@ -35,7 +35,8 @@ PF_KEYS = dict(T_liquidus=1623.0, gas_const=8.3, Qg=1.4e5, L0=3.5e3, kappa_g=2.7
                ad_hoc=1.0)
 METRIC = "cell_orientation_updates_per_s"
 UNIT = "cell*ori/s"
-KERNEL = "pf_tma_kernel<ANISO=true, TSRC=heat, 256> (fused heat + anisotropic phase field)"
+KERNEL = ("pf_tma_kernel<ANISO=true, TSRC=heat, 256, VEC=4, FIX=1> (fused heat + anisotropic "
+          "phase field, compile-time 24x10 tile plan)")
 
 
 def gamma_args(w):
