@@ -208,7 +208,9 @@ int pfg_device_error(int clear);
  * 1 = rows per warp (1..32), 2 = shared-memory plane slots (4..6),
  * 3 = z chunks per tile column, 5 = consumer threads of the TMA-fed kernel
  * (256: two CTAs per SM; 512: one larger CTA per SM), 6 = cells per thread of
- * the CFD solver's kernels (1..16, default 4).  Process-wide; the stencil
+ * the CFD solver's kernels (1..16, default 4), 7 = 1 to run the TMA-fed
+ * kernel's compile-time plans (pfg_fixed_plan) through its run-time-plan
+ * instance instead.  Process-wide; the stencil
  * steps' results do not change; the CFD solver's dot products are summed in
  * another order (float64 rounding only). */
 int pfg_tune(int key, int value);
@@ -219,6 +221,12 @@ int pfg_tune(int key, int value);
  * unit, CTAs, dynamic shared memory bytes, SM count.  kernel: 1 generic,
  * 2 cp.async warp-per-cells, 3 TMA-fed. */
 int pfg_describe_plan(const pfg_pf_params* p, int32_t* out);
+
+/* Which compile-time tile plan the TMA-fed kernel runs for these parameters
+ * on the current device: 1 (num_oris = 20, 24 x 10 tiles), 2 (num_oris = 30,
+ * 16 x 9 tiles), or 0 (the plan is read at run time; also when another
+ * kernel runs).  A negative value is -pfg_status. */
+int pfg_fixed_plan(const pfg_pf_params* p);
 
 /* ---- phase field --------------------------------------------------------
  * One explicit Euler step of the Allen-Cahn grain-growth model with the

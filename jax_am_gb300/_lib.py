@@ -137,6 +137,7 @@ _PROTOS = {
     "pfg_device_error": (_I, [_I]),
     "pfg_tune": (_I, [_I, _I]),
     "pfg_describe_plan": (_I, [ctypes.POINTER(PfParams), _P]),
+    "pfg_fixed_plan": (_I, [ctypes.POINTER(PfParams)]),
     "pfg_pf_step": (_I, [ctypes.POINTER(PfParams), _P, _P, _P, _F, _P]),
     "pfg_pf_step_quench": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(Quench), _P, _P, _P, _P,
                                 _F, _P]),
@@ -241,7 +242,12 @@ def describe_plan(params):
     """The launch plan of a step with ``params`` on the current device."""
     out = (ctypes.c_int32 * 12)()
     check(load().pfg_describe_plan(ctypes.byref(params), out), "pfg_describe_plan")
-    return dict(zip(PLAN_FIELDS, list(out)))
+    plan = dict(zip(PLAN_FIELDS, list(out)))
+    fixed = load().pfg_fixed_plan(ctypes.byref(params))
+    if fixed < 0:
+        check(-fixed, "pfg_fixed_plan")
+    plan["fixed"] = fixed  # compile-time tile plan of the TMA-fed kernel (0: none)
+    return plan
 
 
 def device_error(clear=True):

@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(kThreads, 2) pf_warp_kernel(const __grid_const
 
 extern int g_tma_consumers;
 extern int g_cfd_cells_per_thread;
+extern int g_fixed_plans;
 // Plan overrides for tuning sweeps (0 = automatic).
 static int g_tune_wx = 0, g_tune_rpw = 0, g_tune_stages = 0, g_tune_zchunks = 0;
 
@@ -64,6 +65,8 @@ int set_tune(int key, int value) {
             g_tma_consumers = value ? value : 256; return PFG_OK;
     case 6: if (value > 16) return PFG_ERR_PARAM;
             g_cfd_cells_per_thread = value ? value : 4; return PFG_OK;
+    case 7: if (value > 1) return PFG_ERR_PARAM;
+            g_fixed_plans = value ? 0 : 1; return PFG_OK;
     default: return PFG_ERR_PARAM;
   }
 }

@@ -524,6 +524,19 @@ extern "C" int pfg_describe_plan(const pfg_pf_params* p, int32_t* out) {
   return PFG_OK;
 }
 
+extern "C" int pfg_fixed_plan(const pfg_pf_params* p) {
+  int st = check_pf_params(p);
+  if (st) return -st;
+  if (!device_info().ok) return -PFG_ERR_NO_DEVICE;
+  const DeviceInfo& d = device_info();
+  TilePlan t;
+  const int variant = g_kernel_variant;
+  if ((variant == 0 || variant == 3) &&
+      plan_tma_tiles(p->nx, p->ny, p->nz, p->num_oris, p->bc_x, d.sm_count, d.smem_per_sm, &t))
+    return fixed_plan_index(p->num_oris, t);
+  return 0;
+}
+
 extern "C" int pfg_device_error(int clear) {
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
   const int v = read_device_error(clear);

@@ -123,24 +123,33 @@ __device__ __forceinline__ float4 tma_fold(const PFConsts& c, const TempCoef& tc
 // bulk copy starts on a 16-byte boundary and moves a multiple of 16 bytes
 // without leaving the grid row, and the tile's first cell sits at position
 // x0 - base of the staged row.
-// The launch plan of the common large-grid case with 20 orientations (every
-// configuration of the reference uses num_oris = 20): 24 x 10 cell tiles,
-// 6 cells x 5 lanes per warp row, 5 rows per warp, 4 ring slots.  With
-// FIX = 1 the kernel takes these as compile-time constants (the host launches
-// it only for exactly this plan), which folds the tile arithmetic into
-// immediate offsets.
-struct FixedPlan20 {
-  static constexpr int n = 20, tx = 24, ty = 10, rpw = 5, cpw = 6, wx = 4, tpc = 5, stages = 4;
-  static constexpr int pitch = (tx + 2) * n, tslot = ((ty + 2) * (tx + 2) + 3) / 4 * 4;
+// Launch plans the planner picks for the reference's large workloads, as
+// compile-time constants: FIX = 1 is the 20-orientation case (every
+// configuration of the reference uses num_oris = 20; 24 x 10 cell tiles,
+// 6 cells x 5 lanes per warp row, 5 rows per warp), FIX = 2 the 30-orientation
+// multi-track case (8-byte vectors, 16 x 9 tiles, 2 cells x 15 lanes per warp
+// row, 9 rows per warp); both with 4 ring slots and 256 threads.  The host
+// launches an instance only for exactly its plan; the tile arithmetic then
+// folds into immediate offsets.
+template <int FIX> struct FixedPlan;
+template <> struct FixedPlan<1> {
+  static constexpr int vec = 4, n = 20, tx = 24, ty = 10, rpw = 5, cpw = 6, wx = 4, tpc = 5;
+  static constexpr int stages = 4, pitch = (tx + 2) * n, tslot = ((ty + 2) * (tx + 2) + 3) / 4 * 4;
+};
+template <> struct FixedPlan<2> {
+  static constexpr int vec = 2, n = 30, tx = 16, ty = 9, rpw = 9, cpw = 2, wx = 8, tpc = 15;
+  // 8-byte-vector rows carry two more cells (the even-aligned copy range)
+  static constexpr int stages = 4, pitch = ((tx + 4) * n + 3) / 4 * 4;
+  static constexpr int tslot = ((ty + 2) * (tx + 2) + 3) / 4 * 4;
 };
 
 template <bool ANISO, int TSRC, int NC, int VEC, int FIX>
 __global__ void __launch_bounds__(NC, NC == 256 ? 2 : 1)
 pf_tma_kernel(const __grid_constant__ StepArgs a) {
   static_assert(VEC == 4 || VEC == 2, "16- or 8-byte vectors");
-  static_assert(FIX == 0 || (VEC == 4 && NC == 256), "the fixed plan is a 16-byte, 256-thread plan");
-  using FP = FixedPlan20;
-  constexpr bool kFix = FIX == 1;
+  using FP = FixedPlan<FIX == 0 ? 1 : FIX>;
+  static_assert(FIX == 0 || (FP::vec == VEC && NC == 256), "a fixed plan is a 256-thread plan");
+  constexpr bool kFix = FIX != 0;
   // tile plan: compile-time constants under FIX, the launch arguments otherwise
   const int P_n = kFix ? FP::n : a.n, P_pitch = kFix ? FP::pitch : a.pitch;
   const int P_tx = kFix ? FP::tx : a.tx, P_ty = kFix ? FP::ty : a.ty;
@@ -541,10 +550,26 @@ static cudaError_t launch_tma_t(const StepArgs& a, const TilePlan& t, cudaStream
   return cudaGetLastError();
 }
 
-// the plan is exactly FixedPlan20
-static bool is_fixed_plan20(const StepArgs& a, const TilePlan& t) {
-  using FP = FixedPlan20;
-  return t.rs == 256 && t.vec == 4 && a.n == FP::n && t.tx == FP::tx && t.ty == FP::ty &&
+// the plan is exactly FixedPlan<FIX>
+template <int FIX>
+static bool plan_is(int n, const TilePlan& t) {
+  using FP = FixedPlan<FIX>;
+  return t.rs == 256 && t.vec == FP::vec && n == FP::n && t.tx == FP::tx && t.ty == FP::ty &&
+         t.rpw == FP::rpw && t.cpw == FP::cpw && t.wx == FP::wx && t.tpc == FP::tpc &&
+         t.stages == FP::stages && t.pitch == FP::pitch && t.tslot == FP::tslot;
+}
+
+extern int g_fixed_plans;
+int fixed_plan_index(int n, const TilePlan& t) {
+  if (!g_fixed_plans) return 0;
+  return plan_is<1>(n, t) ? 1 : (plan_is<2>(n, t) ? 2 : 0);
+}
+
+// ... and the launch arguments carry exactly that plan
+template <int FIX>
+static bool is_fixed_plan(const StepArgs& a, const TilePlan& t) {
+  using FP = FixedPlan<FIX>;
+  return t.rs == 256 && t.vec == FP::vec && a.n == FP::n && t.tx == FP::tx && t.ty == FP::ty &&
          t.rpw == FP::rpw && t.cpw == FP::cpw && t.wx == FP::wx && t.tpc == FP::tpc &&
          t.stages == FP::stages && t.pitch == FP::pitch && t.tslot == FP::tslot &&
          a.pitch == FP::pitch && a.tx == FP::tx && a.ty == FP::ty && a.rpw == FP::rpw &&
@@ -552,11 +577,16 @@ static bool is_fixed_plan20(const StepArgs& a, const TilePlan& t) {
          a.tslot == FP::tslot;
 }
 
+int g_fixed_plans = 1;  // pfg_tune key 7: 0 runs every plan through the run-time-plan instance
+
 template <int TSRC>
 cudaError_t launch_tma_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s) {
-  if (is_fixed_plan20(a, t))
+  if (g_fixed_plans && is_fixed_plan<1>(a, t))
     return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 256, 4, 1>(a, t, s)
                               : launch_tma_t<false, TSRC, 256, 4, 1>(a, t, s);
+  if (g_fixed_plans && is_fixed_plan<2>(a, t))
+    return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 256, 2, 2>(a, t, s)
+                              : launch_tma_t<false, TSRC, 256, 2, 2>(a, t, s);
   if (t.rs == 512)
     return (a.pc.aniso > 0.f) ? launch_tma_t<true, TSRC, 512, 4>(a, t, s)
                               : launch_tma_t<false, TSRC, 512, 4>(a, t, s);

@@ -54,6 +54,8 @@ bool plan_tma_tiles(int nx, int ny, int nz, int n, int bcx, int sm_count, int ma
                     TilePlan* out);
 template <int TSRC>
 cudaError_t launch_tma_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);
+// Which compile-time plan of the TMA-fed kernel (1 or 2) a TMA plan uses, or 0.
+int fixed_plan_index(int n, const TilePlan& t);
 // The device error flag (PFG_ERR_TIMEOUT after a bounded wait ran out), or a
 // negative pfg_status if it cannot be read; clear != 0 resets it.
 int read_device_error(int clear);

@@ -154,8 +154,8 @@ def _assert_fixed_plan(pf_args, poly):
     from jax_am_gb300.phase_field.allen_cahn import make_pf_params
     p = _lib.describe_plan(make_pf_params(pf_args, poly))
     got = (p["kernel"], p["vec"], p["tile_x"], p["tile_y"], p["rows_per_warp"], p["warps_x"],
-           p["slots"])
-    assert got == (3, 4, 24, 10, 5, 4, 4), p
+           p["slots"], p["fixed"])
+    assert got == (3, 4, 24, 10, 5, 4, 4, 1), p
 
 
 def test_fixed_plan_fused_laser_vs_oracle():
@@ -199,3 +199,42 @@ def test_fixed_plan_T_array_vs_oracle(aniso):
     for _ in range(3):
         e = e + dt * PT.pf_increment(e, T3, a, _dirs(poly))
     _compare(f"fixed 24x10 plan, T array, A={aniso}", state[0], e)
+
+
+def test_fixed_plan30_vs_oracle():
+    """320 x 160 x 80 cells with n = 30 (8-byte vectors): the compile-time
+    16 x 9 plan (FixedPlan<2>) of the multi-track configuration; three
+    temperature-array steps and 10 fused heat + anisotropic steps against the
+    float64 oracle."""
+    from jax_am_gb300 import _lib
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver, make_pf_params
+    from jax_am_gb300.phase_field.utils import Field
+    from jax_am_gb300.runner import single_track
+    nx, ny, nz = 320, 160, 80
+    pf_args = dict(PF_KEYS, Nx=nx, Ny=ny, Nz=nz, h=1e-6, num_grains=400, num_oris=30,
+                   T_liquidus=1623.0, anisotropy=0.15)
+    poly = Field(pf_args, seed=8)
+    p = _lib.describe_plan(make_pf_params(pf_args, poly))
+    assert (p["kernel"], p["vec"], p["tile_x"], p["tile_y"], p["rows_per_warp"], p["warps_x"],
+            p["fixed"]) == (3, 2, 16, 9, 9, 8, 2), p
+    s = PFSolver(pf_args, poly)
+    g = torch.Generator(device="cuda").manual_seed(9)
+    e0 = s.ini_cond()
+    e0 = torch.clamp(e0 + 0.3 * torch.rand(e0.shape, generator=g, device="cuda"), 0.0, 1.0)
+    T = 1450.0 + 300.0 * torch.rand((s.N, 1), generator=g, device="cuda")
+    dt = float(np.float32(1e-8))
+    state = (e0.clone(), 0.0)
+    for k in range(3):
+        state, _ = s.stepper(state, (k + 1) * dt, [T])
+    a = _oracle_args(pf_args, poly)
+    e = e0.double().reshape(nz, ny, nx, -1)
+    T3 = T.double().reshape(nz, ny, nx)
+    for _ in range(3):
+        e = e + dt * PT.pf_increment(e, T3, a, _dirs(poly))
+    _compare("fixed 16x9 plan, T array, n=30", state[0], e)
+    del state, e, e0, T, T3, s
+    torch.cuda.empty_cache()
+    path = single_track(20e-6, 80e-6, 0.8, 200.0, 1.0)
+    Tmax = _laser_case((nx, ny, nz), 30, 400, 0.15, path, 10, 8,
+                       "fixed 16x9 plan, 320x160x80 n=30 A=0.15, 10 fused steps")
+    assert Tmax > 300.0
