@@ -148,7 +148,7 @@ def test_multi_track_laser_reduced():
 
 
 def _assert_fixed_plan(pf_args, poly):
-    """The step kernel takes the compile-time 24 x 10 plan (FixedPlan20 in
+    """The step kernel takes the compile-time 24 x 10 plan (FixedPlan<1> in
     pf_tma.cu) exactly when the planner picks this plan."""
     from jax_am_gb300 import _lib
     from jax_am_gb300.phase_field.allen_cahn import make_pf_params
