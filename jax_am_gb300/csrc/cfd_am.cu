@@ -40,6 +40,8 @@ struct Dims {
   int nx, ny, nz;
   long long n;
   double D[6], dS[6], dV;  // mesh3d's signed face distances and areas (cfd_am.py:681-690)
+  double g[6];             // dS / D per face, computed once on the host
+  double invD[6];          // 1 / D: the kernels multiply (float64 division is slow on GB300)
 };
 
 static Dims make_dims(const pfg_cfd_grid& g) {
@@ -54,6 +56,8 @@ static Dims make_dims(const pfg_cfd_grid& g) {
   for (int f = 0; f < 6; ++f) {
     d.D[f] = D[f];
     d.dS[f] = S[f];
+    d.g[f] = S[f] / D[f];
+    d.invD[f] = 1.0 / D[f];
   }
   d.dV = dx * dy * dz;
   return d;
@@ -523,7 +527,7 @@ __global__ void k_energy_residual(Dims d, EnergyK K, const double* U, const doub
       const double un = U[nb_index(d, c, i, j, k, f)];
       const double kn = linclip(e.k, un);
       const double mu = 2.0 * ku * kn / (kn + ku);
-      lap += (un - u) / d.D[f] * mu * d.dS[f];
+      lap += (un - u) * d.invD[f] * mu * d.dS[f];
     }
     const double t0 = T0[c];
     const double cp0 = cp_eff(e, t0);
@@ -568,11 +572,11 @@ __global__ void k_energy_jacobian(Dims d, EnergyK K, const double* U, const doub
     for (int f = 0; f < 6; ++f) {
       const double un = U[nb_index(d, c, i, j, k, f)];
       const double kn = linclip(e.k, un), dkn = linclip_d(e.k, un);
-      const double den = kn + ku;
-      const double mu = 2.0 * ku * kn / den;
-      const double dmu_p = 2.0 * dku * kn * kn / (den * den);
-      const double dmu_n = 2.0 * dkn * ku * ku / (den * den);
-      const double g = d.dS[f] / d.D[f];
+      const double rden = 1.0 / (kn + ku);  // one float64 division per face
+      const double mu = 2.0 * ku * kn * rden;
+      const double dmu_p = 2.0 * dku * kn * kn * (rden * rden);
+      const double dmu_n = 2.0 * dkn * ku * ku * (rden * rden);
+      const double g = d.g[f];
       v0 += g * mu - (un - u) * g * dmu_p;
       const double vf = -(g * mu + (un - u) * g * dmu_n);
       vals[(1 + f) * d.n + c] = vf;
@@ -640,14 +644,14 @@ __global__ void k_momentum(Dims d, FlowK F, int comp, const double* T, const dou
     double v0 = 0.0, dg = 0.0;
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-      const double gq = d.dS[q] / d.D[q];
+      const double gq = d.g[q];
       v0 += gq * f.visco;
       const double vq = -gq * f.visco;
       vals[(1 + q) * d.n + c] = vq;
       if (on_face(d, i, j, k, q)) {
         dg += vq;
         // Dirichlet walls: all faces but the top for u and v (cfd_am.py:304-310)
-        if (q < 5 || comp == 2) v0 += f.visco * 2.0 / d.D[q] * d.dS[q];
+        if (q < 5 || comp == 2) v0 += f.visco * 2.0 * d.invD[q] * d.dS[q];
       }
     }
     v0 += (f.rho / f.dt + darcy) * d.dV;
@@ -662,7 +666,7 @@ __global__ void k_pressure_vals(Dims d, double* vals) {
     double v0 = 0.0;
 #pragma unroll
     for (int q = 0; q < 6; ++q) {
-      const double gq = d.dS[q] / d.D[q];
+      const double gq = d.g[q];
       v0 += gq;
       vals[(1 + q) * d.n + c] = -gq;
     }
