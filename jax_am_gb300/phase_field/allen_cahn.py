@@ -98,6 +98,20 @@ def as_device_f32(x, shape=None, name="array"):
     return x
 
 
+class PendingMetrics:
+    """The metrics record of ``PFSolver.inspect_async``, read on demand."""
+
+    def __init__(self, solver, host, event):
+        self._solver, self._host, self._event = solver, host, event
+
+    def done(self):
+        return self._event.query()
+
+    def result(self):
+        self._event.synchronize()
+        return self._solver._metrics(_lib.Diag.from_buffer_copy(self._host.numpy().tobytes()))
+
+
 class PFSolver:
     """Explicit-Euler Allen-Cahn grain growth on one GPU
     (reference: ``allen_cahn.py:131-210``)."""
@@ -236,7 +250,7 @@ class PFSolver:
         self._diag(eta, torch.zeros(self.N, device="cuda"), None, out, ghosted=False)
         return out
 
-    def _diag(self, eta, T, argmax0, argmax_out, ghosted, entry="pfg_pf_diag"):
+    def _diag_launch(self, eta, T, argmax0, argmax_out, ghosted, entry):
         if self._diag_scratch is None:
             nbytes = self.lib.pfg_pf_diag_scratch_bytes(ctypes.byref(self.params))
             self._diag_scratch = torch.empty(max(int(nbytes), 16), dtype=torch.uint8,
@@ -248,17 +262,13 @@ class PFSolver:
                                   _lib.ptr(self._diag_scratch), self._diag_scratch.numel(),
                                   _lib.ptr(self._diag_out), _stream())
         _lib.check(st, entry)
+
+    def _diag(self, eta, T, argmax0, argmax_out, ghosted, entry="pfg_pf_diag"):
+        self._diag_launch(eta, T, argmax0, argmax_out, ghosted, entry)
         host = self._diag_out.cpu().numpy()
         return _lib.Diag.from_buffer_copy(host.tobytes())
 
-    def inspect(self, eta, T, eta0=None, T_ghosted=False):
-        """The reference's inspect_sol metrics only (argmax changes, liquid
-        fraction, max T, NaN count), one pass over eta on the GPU."""
-        return self.diagnostics(eta, T, eta0, T_ghosted, _entry="pfg_pf_inspect")
-
-    def diagnostics(self, eta, T, eta0=None, T_ghosted=False, _entry="pfg_pf_diag"):
-        """Energy, mass, liquid fraction, argmax changes and NaN count of a
-        state, reduced on the GPU (compensated accumulation)."""
+    def _diag_inputs(self, eta, T, eta0):
         eta = as_device_f32(eta, (self.N, self.n), "eta")
         T = as_device_f32(T, None, "T")
         a0 = None
@@ -267,7 +277,36 @@ class PFSolver:
                 self._argmax0 = self.argmax(as_device_f32(eta0, (self.N, self.n), "eta0"))
                 self._argmax0_src = eta0
             a0 = self._argmax0
-        d = self._diag(eta, T, a0, None, T_ghosted, _entry)
+        return eta, T, a0
+
+    def inspect(self, eta, T, eta0=None, T_ghosted=False):
+        """The reference's inspect_sol metrics only (argmax changes, liquid
+        fraction, max T, NaN count), one pass over eta on the GPU."""
+        return self.diagnostics(eta, T, eta0, T_ghosted, _entry="pfg_pf_inspect")
+
+    def inspect_async(self, eta, T, eta0=None, T_ghosted=False):
+        """``inspect`` without waiting for it: the metrics kernel and a copy of
+        its record to pinned host memory are enqueued on the current stream,
+        and ``result()`` of the returned ``PendingMetrics`` waits for them and
+        gives ``inspect``'s dict.  Work enqueued later on the same stream runs
+        after the kernel has read ``eta`` and ``T``, so a driver can launch
+        its next steps first and read these metrics while they run (the
+        reference's ``inspect_sol`` is synchronous: ``inspect``)."""
+        eta, T, a0 = self._diag_inputs(eta, T, eta0)
+        self._diag_launch(eta, T, a0, None, T_ghosted, "pfg_pf_inspect")
+        host = torch.empty(self._diag_out.numel(), dtype=torch.uint8, pin_memory=True)
+        host.copy_(self._diag_out, non_blocking=True)
+        event = torch.cuda.Event()
+        event.record()
+        return PendingMetrics(self, host, event)
+
+    def diagnostics(self, eta, T, eta0=None, T_ghosted=False, _entry="pfg_pf_diag"):
+        """Energy, mass, liquid fraction, argmax changes and NaN count of a
+        state, reduced on the GPU (compensated accumulation)."""
+        eta, T, a0 = self._diag_inputs(eta, T, eta0)
+        return self._metrics(self._diag(eta, T, a0, None, T_ghosted, _entry))
+
+    def _metrics(self, d):
         N = max(int(d.n_cells), 1)
         return {
             "energy": d.energy, "max_T": d.max_T, "n_cells": d.n_cells,

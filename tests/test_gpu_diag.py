@@ -74,3 +74,25 @@ def test_inspect_matches_full_diagnostics(shape, n, bc):
     assert light["energy"] == 0.0 and not np.any(light["mass"])
     m = O.inspect(eta, eta0, T, oargs["T_liquidus"])
     assert light["pct_liquid"] == pytest.approx(m["pct_liquid"], abs=1e-12)
+
+
+def test_inspect_async_is_ordered_before_later_steps():
+    """inspect_async's record is the state it was given even when further
+    steps are enqueued before result() is read; it equals inspect's."""
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    from jax_am_gb300.runner import HeatPFRun, single_track
+    from tests.cases import GAMMA_DEFAULTS
+    poly, eta, _, pf_args, _, _ = pf_case((48, 32, 16), 20, 0.15, seed=3, h=(1e-6,) * 3)
+    s = PFSolver(pf_args, poly)
+    run = HeatPFRun(s, dict(GAMMA_DEFAULTS), single_track(5e-6, 16e-6, 0.8, 200.0, 1e-3),
+                    dt=2e-9, eta0=torch.tensor(eta, dtype=torch.float32, device="cuda"))
+    run.run(20)
+    ref = s.inspect(run.state, run.T_ghosted, eta0=eta, T_ghosted=True)
+    pend = s.inspect_async(run.state, run.T_ghosted, eta0=eta, T_ghosted=True)
+    run.run(40)  # overwrites both state buffers before the record is read
+    got = pend.result()
+    later = s.inspect(run.state, run.T_ghosted, eta0=eta, T_ghosted=True)
+    for k in ("max_T", "n_cells", "n_ori_changed", "n_liquid", "n_nonfinite"):
+        assert got[k] == ref[k], k
+    assert later["max_T"] != ref["max_T"]  # the later state differs
+    assert pend.done()
