@@ -205,3 +205,26 @@ def test_am3d_local_spacing_differs():
             ok, err, scale = close(getattr(s, f), getattr(o, f), 1e-7)
             assert ok, (step, f, err, scale)
     assert float(s.T.max()) > 1623.0 and float(s.vel.abs().max()) > 0.0
+
+
+@pytest.mark.parametrize("N,NL,heat_source", [([10, 8, 5], [10, 8, 5], 0),
+                                              ([9, 7, 1], [5, 4, 1], 0),
+                                              ([12, 9, 6], [12, 9, 6], 1)])
+def test_am3d_edge_shapes(N, NL, heat_source):
+    """A flow box equal to the whole grid (the reference's drivers allow
+    mesh_local = mesh, applications/cfd/simple/example.py:30) and a single
+    layer of cells (top and bottom faces on the same cells): two steps
+    against the oracle."""
+    h = 5e-6
+    args = dict(CASES["surface"] if heat_source == 0 else CASES["body"], P=40.0, speed=2.5,
+                X0=[2e-5, 2e-5, N[2] * h])
+    cp, k = (0.2441, 338.39, 300.0, 1563.0), (0.0163105, 4.5847, 300.0, 1563.0)
+    s = gpu_solver(args, N, NL, h, cp, k)
+    o = oracle_solver(args, N, NL, h, cp, k)
+    for step in range(2):
+        s.time_integration()
+        o.time_integration()
+        torch.cuda.synchronize()
+        for f in FIELDS:
+            ok, err, scale = close(getattr(s, f), getattr(o, f), 1e-7)
+            assert ok, (N, NL, step, f, err, scale)
