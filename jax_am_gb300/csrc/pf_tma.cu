@@ -81,9 +81,13 @@ __device__ __forceinline__ void tma_row(void* dst, const void* src, unsigned byt
 
 // Folded update of one element (see pfg_warp.cuh for the derivation).  The
 // per-cell coefficients are k = (A1, B1, C1, W) with W = -C2 = 2 A cl w_x, and
-// the anisotropy enters through cn = -min(cos^2, 1) = max(m * rcp(-ee), -1):
-// C1 + C2 c2 (1 - c2) = C1 + W (cn + cn^2).  |e| = 0 gives m * rcp(-0) = NaN,
-// fmaxf(NaN, -1) = -1 and cn + cn^2 = 0, the reference's NaN-to-zero rule.
+// the anisotropy enters through cn = -cos^2 = m * rcp(-ee):
+// C1 + C2 c2 (1 - c2) = C1 + W (cn + cn^2).  ee starts from 1e-30 instead of
+// 0, so |e| = 0 gives m = 0, cn = 0 and cn + cn^2 = 0: the value of the
+// reference's NaN-to-zero rule (cos^2 = 1), with no clamp.  For any gradient
+// that matters, ee >= ~1e-14 and the 1e-30 is far below an ulp; rounding can
+// leave m / ee a few ulps above 1, which changes the anisotropy term by a
+// relative ~1e-7 instead of clamping it to 0.
 struct LapConstsT {
   float ry, rz, nm;
 };
@@ -95,14 +99,14 @@ __device__ __forceinline__ float tma_update_elem(const LapConstsT& L, float e, f
   float u = k.z;
   if constexpr (ANISO) {
     const float ex = xp - xm, ey = yp - ym, ez = zp - zm;
-    const float ee = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+    const float ee = fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, 1e-30f)));
     const float p0 = fmaf(d[0], ex, fmaf(d[1], ey, d[2] * ez));
     const float p1 = fmaf(d[3], ex, fmaf(d[4], ey, d[5] * ez));
     const float q0 = p0 * p0, q1 = p1 * p1;
     const float q2 = ee - q0 - q1;
     float m;
     asm("max.f32 %0, %1, %2, %3;" : "=f"(m) : "f"(q0), "f"(q1), "f"(q2));
-    const float cn = fmaxf(m * rcp_approx(-ee), -1.f);
+    const float cn = m * rcp_approx(-ee);
     u = fmaf(k.w, fmaf(cn, cn, cn), k.z);
   }
   return fmaf(u, lap, e * fmaf(k.y, e * e, k.x));
