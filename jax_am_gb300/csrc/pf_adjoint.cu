@@ -88,6 +88,8 @@ __device__ __forceinline__ float cell_sum(float v, const AdjLanes& l) {
 }
 
 // ---- kernel A: u, v, the local term and the temperature sensitivity --------
+// ANISO = false (A = 0): v is identically zero and is neither written nor read.
+template <bool ANISO>
 __global__ void __launch_bounds__(256) adj_pf_local_kernel(const __grid_constant__ AdjArgs a) {
   const int ncell = a.nx * a.ny * a.nz;  // host checks < 2^31
   const int n = a.n;
@@ -154,7 +156,7 @@ __global__ void __launch_bounds__(256) adj_pf_local_kernel(const __grid_constant
         const float L = a.pc.wx * ((vxp - e) + (vxm - e)) + a.pc.wy * ((vyp - e) + (vym - e)) +
                         a.pc.wz * ((vzp - e) + (vzm - e));
         float an = 1.f, dax = 0.f, day = 0.f, daz = 0.f;
-        if (A > 0.f) {
+        if (ANISO) {
           const float ex = vxp - vxm, ey = vyp - vym, ez = vzp - vzm;
           const float ee = ex * ex + ey * ey + ez * ez;
           float pbest = 0.f, m = -1.f;
@@ -182,9 +184,11 @@ __global__ void __launch_bounds__(256) adj_pf_local_kernel(const __grid_constant
         const float gg = e * (K - 3.f * e * e);
         const float Q = Lg * kap;
         a.u[base + i] = lam * Q * an;
-        a.v[base + i] = lam * Q * L * dax;
-        a.v[Nn + base + i] = lam * Q * L * day;
-        a.v[2 * Nn + base + i] = lam * Q * L * daz;
+        if (ANISO) {
+          a.v[base + i] = lam * Q * L * dax;
+          a.v[Nn + base + i] = lam * Q * L * day;
+          a.v[2 * Nn + base + i] = lam * Q * L * daz;
+        }
         a.loc[base + i] = liquid ? 0.f : -Lg * mg * (lam * (K - 9.f * e * e) + 8.f * e * ld);
         mu += lam * (dLg * (-mg * gg + kap * an * L) + Lg * mg * 4.f * om * e * dz);
       }
@@ -198,6 +202,7 @@ __global__ void __launch_bounds__(256) adj_pf_local_kernel(const __grid_constant
 }
 
 // ---- kernel B: the adjoint of the stencil terms, gathered per element --------
+template <bool ANISO>
 __global__ void __launch_bounds__(256) adj_pf_gather_kernel(const __grid_constant__ AdjArgs a) {
   const int ncell = a.nx * a.ny * a.nz;
   const int n = a.n;
@@ -236,9 +241,12 @@ __global__ void __launch_bounds__(256) adj_pf_gather_kernel(const __grid_constan
       const float lapu = a.pc.wx * (a.u[off[0] + i] + a.u[off[1] + i] - 2.f * uc) +
                          a.pc.wy * (a.u[off[2] + i] + a.u[off[3] + i] - 2.f * uc) +
                          a.pc.wz * (a.u[off[4] + i] + a.u[off[5] + i] - 2.f * uc);
-      const float dvx = sgn[1] * a.v[off[1] + i] - sgn[0] * a.v[off[0] + i];
-      const float dvy = sgn[3] * a.v[Nn + off[3] + i] - sgn[2] * a.v[Nn + off[2] + i];
-      const float dvz = sgn[5] * a.v[2 * Nn + off[5] + i] - sgn[4] * a.v[2 * Nn + off[4] + i];
+      float dvx = 0.f, dvy = 0.f, dvz = 0.f;
+      if (ANISO) {
+        dvx = sgn[1] * a.v[off[1] + i] - sgn[0] * a.v[off[0] + i];
+        dvy = sgn[3] * a.v[Nn + off[3] + i] - sgn[2] * a.v[Nn + off[2] + i];
+        dvz = sgn[5] * a.v[2 * Nn + off[5] + i] - sgn[4] * a.v[2 * Nn + off[4] + i];
+      }
       a.lam_out[base + i] =
           m * a.lam_in[base + i] + a.dt * (a.loc[base + i] + lapu - (dvx + dvy + dvz));
     }
@@ -439,10 +447,13 @@ extern "C" int pfg_adjoint_step(const pfg_pf_params* p, const pfg_heat_params* h
   const int cpw = 32 / ((p->num_oris + 1) / 2);  // cells per warp of kernels A and B
   const int warps_blocks =
       (int)std::min<int64_t>((N + 8 * cpw - 1) / (8 * cpw), (int64_t)d.sm_count * 16);
-  adj_pf_local_kernel<<<warps_blocks, 256, 0, s>>>(a);
+  const bool aniso = a.pc.aniso > 0.f;
+  if (aniso) adj_pf_local_kernel<true><<<warps_blocks, 256, 0, s>>>(a);
+  else adj_pf_local_kernel<false><<<warps_blocks, 256, 0, s>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return record_cuda(e);
-  adj_pf_gather_kernel<<<warps_blocks, 256, 0, s>>>(a);
+  if (aniso) adj_pf_gather_kernel<true><<<warps_blocks, 256, 0, s>>>(a);
+  else adj_pf_gather_kernel<false><<<warps_blocks, 256, 0, s>>>(a);
   e = cudaGetLastError();
   if (e != cudaSuccess) return record_cuda(e);
   const int cell_blocks = (int)std::min<int64_t>((N + 255) / 256, (int64_t)d.sm_count * 16);
