@@ -116,6 +116,10 @@ class LaserTrackProblem:
         nbytes = int(self.lib.pfg_adjoint_scratch_bytes(ctypes.byref(self.p)))
         scratch = torch.empty(nbytes // 4 + 1, dtype=torch.float32, device="cuda")
         dt = self.dt
+        # the device clock at each step: float32 dt summed in float64, in order
+        times = [0.0]
+        for _ in range(self.steps):
+            times.append(times[-1] + dt)
         for seg in reversed(range(len(self._ckpt))):
             k0 = seg * self.C
             nseg = min(self.C, self.steps - k0)
@@ -125,9 +129,7 @@ class LaserTrackProblem:
                       keep=lambda k, e, T, c: states.append((e.clone(), T.clone())))
             for j in reversed(range(nseg)):
                 k = k0 + j
-                t = 0.0
-                for _ in range(k):  # the device clock sums float32 dt in float64
-                    t += dt
+                t = times[k]
                 e_k, T_k = states[j]
                 st = self.lib.pfg_adjoint_step(
                     ctypes.byref(self.p), ctypes.byref(h), _lib.ptr(e_k), _lib.ptr(T_k), t, dt,
