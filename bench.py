@@ -360,6 +360,38 @@ def time_cpu_baseline(w, budget_s=15.0, threads=None, sample=(100, 50, 25), step
                       f"{el:.1f} s"}
 
 
+def time_cpu_numpy(w, budget_s=8.0, sample=(50, 25, 13), steps_max=10):
+    """The float64 NumPy oracle (``oracle/pf_oracle.py``, the restatement the
+    parity tests check against) on the same physics, a smaller bounded sample:
+    the second CPU reference point beside the float32 PyTorch port."""
+    from oracle import pf_oracle as O
+    from jax_am_gb300.phase_field.utils import grain_directions, random_quaternions
+    nx, ny, nz = sample
+    n = w["num_oris"]
+    rng = np.random.default_rng(0)
+    args = dict(PF_KEYS, Nx=nx, Ny=ny, Nz=nz, anisotropy=w["anisotropy"], h=(w["h"],) * 3,
+                num_oris=n)
+    dirs = grain_directions(random_quaternions(n, rng)).astype(np.float64)
+    eta = np.zeros((nx * ny * nz, n))
+    eta[np.arange(nx * ny * nz), rng.integers(0, n, nx * ny * nz)] = 1.0
+    Tg = np.full((nx + 2, ny + 2, nz + 2), w["T0"])
+    g = gamma_args(w)
+    dt = 3e-8
+
+    def laser(t):
+        return 20e-6 + w["speed"] * t, 0.5 * ny * w["h"], w["power"]
+
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < steps_max and (steps == 0 or time.perf_counter() - t0 < budget_s):
+        eta, Tg = O.coupled_step(eta, Tg, steps * dt, dt, args, g, laser, dirs)
+        steps += 1
+    el = time.perf_counter() - t0
+    return {"value": nx * ny * nz * n * steps / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{steps} fused steps of the float64 NumPy oracle (oracle/pf_oracle.py) on "
+                      f"{nx}x{ny}x{nz} cells, n={n}, A={w['anisotropy']}, {el:.1f} s"}
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -513,6 +545,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = time_cpu_baseline(w)
+        cpu["numpy_f64"] = time_cpu_numpy(w)
     serving = None
     if rank == 0 and not args.no_serving:
         serving = time_serving()
