@@ -217,6 +217,48 @@ def time_adjoint():
             "forward_s": t1 - t0, "gradient_s": t2 - t1}
 
 
+def time_heat_step(steps=500):
+    """The standalone explicit heat step (``pfg_heat_step``, the drop-in for
+    ``gamma.update_T``) on the laser-track grid (400 x 200 x 100 interior
+    cells, ghosted float32), both axis orders, ping-pong buffers, CUDA events:
+    microseconds per step and algorithmic bandwidth (read + write 4 bytes per
+    interior cell) against the measured HBM peak."""
+    import ctypes
+    from jax_am_gb300 import _lib
+    from jax_am_gb300.cfd.gamma import make_heat_params
+    lib = _lib.load()
+    w = WORKLOAD
+    nx, ny, nz = w["Nx"], w["Ny"], w["Nz"]
+    peak = measured_peak()[0]
+    out = {"workload": f"{nx}x{ny}x{nz} interior cells, 200 W Gaussian, float32"}
+    for name, layout in (("xyz_reference_order", _lib.LAYOUT_XYZ), ("zyx", _lib.LAYOUT_ZYX)):
+        shape = (nx + 2, ny + 2, nz + 2) if layout == _lib.LAYOUT_XYZ else (nz + 2, ny + 2, nx + 2)
+        a = torch.full(shape, w["T0"], device="cuda")
+        b = a.clone()
+        h = make_heat_params(gamma_args(w), nx, ny, nz, w["h"], w["h"], w["h"], layout=layout)
+        s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+        def step(src, dst):
+            _lib.check(lib.pfg_heat_step(ctypes.byref(h), _lib.ptr(src), _lib.ptr(dst), 50e-6,
+                                         100e-6, w["power"], 2e-9, s), "pfg_heat_step")
+        for _ in range(10):
+            step(a, b)
+            step(b, a)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps // 2):
+            step(a, b)
+            step(b, a)
+        e1.record()
+        torch.cuda.synchronize()
+        us = e0.elapsed_time(e1) / (2 * (steps // 2)) * 1e3
+        gbs = nx * ny * nz * 8 / (us * 1e-6) / 1e9
+        out[name] = {"us_per_step": us, "achieved_GBps": gbs, "roofline_frac": gbs / peak}
+        del a, b
+    return out
+
+
 def time_cfd(steps=20, warmup=3, cpu=False):
     """The implicit CFD solver (``AM_3d``, float64) on the reference's
     standalone CFD driver configuration (``workloads.cfd_simple_case``):
@@ -558,6 +600,9 @@ def main():
     cfd = None
     if rank == 0 and not args.no_cfd:
         cfd = time_cfd(cpu=args.cfd_cpu)
+    heat = None
+    if rank == 0 and not args.no_configs:
+        heat = time_heat_step()
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -573,7 +618,7 @@ def main():
             "gpu_launches": gpu_launches, "clocks": clocks,
             "plan": _lib.describe_plan(solver.params),
             "serving": serving, "adjoint": adjoint, "other_configs": others,
-            "cfd_am3d": cfd,
+            "cfd_am3d": cfd, "heat_step": heat,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

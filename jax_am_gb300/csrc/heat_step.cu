@@ -1,8 +1,10 @@
 // Explicit finite-difference heat step on the ghosted field (jax_am/cfd/gamma.py:55-61).
-// One thread per interior cell; the six neighbours are read straight from the
-// ghosted array (a neighbour across a face is the previous ghost value).  The
-// field may be in either axis order: threadIdx.x runs along the unit-stride
-// axis so loads stay coalesced.
+// A thread owns one (fast, middle) position and marches CH cells along the
+// slowest axis, keeping the previous, current and next values of that axis in
+// registers: per cell it loads the next value and the four in-plane
+// neighbours (a neighbour across a face is the previous ghost value).  The
+// field may be in either axis order; consecutive threads take consecutive
+// cells of the unit-stride axis, so loads stay coalesced.
 #include <cuda_runtime.h>
 
 #include "pfg_device.cuh"
@@ -10,29 +12,43 @@
 
 namespace pfg {
 
+constexpr int kHeatChunk = 8;  // cells marched per thread along the slowest axis
+
 template <bool XYZ>
 __global__ void __launch_bounds__(256)
 heat_step_kernel(const __grid_constant__ HeatConsts H, const float* __restrict__ Tg_in,
                  float* __restrict__ Tg_out, float xl, float yl, float P, float dt) {
-  // (f, m, s) = fastest, middle, slowest thread axes
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  const int m = blockIdx.y * blockDim.y + threadIdx.y;
-  const int s = blockIdx.z;
-  const int gx = XYZ ? s : f, gy = m, gz = XYZ ? f : s;
-  if (gx >= H.nx || gy >= H.ny || gz >= H.nz) return;
-  int64_t sx, sy, sz;
-  if (XYZ) {  // (nx+2, ny+2, nz+2), z fastest: the reference's order
-    sz = 1; sy = H.nz + 2; sx = (int64_t)(H.ny + 2) * (H.nz + 2);
-  } else {    // (nz+2, ny+2, nx+2), x fastest
-    sx = 1; sy = H.nx + 2; sz = (int64_t)(H.ny + 2) * (H.nx + 2);
+  // fast / middle / slow axis extents (XYZ: z, y, x; ZYX: x, y, z)
+  const int nf = XYZ ? H.nz : H.nx, nm = H.ny, ns = XYZ ? H.nx : H.nz;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // host keeps nf * nm < 2^31
+  if (t >= nf * nm) return;
+  const int m = t / nf, f = t - m * nf;
+  const int s0 = blockIdx.y * kHeatChunk;
+  // ghosted strides: unit along the fast axis (host keeps the ghosted size < 2^31)
+  const int sm = nf + 2, ss = (nm + 2) * (nf + 2);
+  int idx = (s0 + 1) * ss + (m + 1) * sm + (f + 1);
+  float prev = __ldg(Tg_in + idx - ss), cur = __ldg(Tg_in + idx);
+  auto cell = [&](int s) {
+    const float next = __ldg(Tg_in + idx + ss);
+    const float fm = __ldg(Tg_in + idx - 1), fp = __ldg(Tg_in + idx + 1);
+    const float mm = __ldg(Tg_in + idx - sm), mp = __ldg(Tg_in + idx + sm);
+    const int gx = XYZ ? s : f, gy = m, gz = XYZ ? f : s;
+    const int sx = XYZ ? ss : 1, sz = XYZ ? 1 : ss;
+    const float Tn = XYZ ? heat_cell_update(H, cur, prev, next, mm, mp, fm, fp, gx, gy, gz, xl,
+                                            yl, P, dt, Tg_out, idx, sx, sm, sz)
+                         : heat_cell_update(H, cur, fm, fp, mm, mp, prev, next, gx, gy, gz, xl,
+                                            yl, P, dt, Tg_out, idx, sx, sm, sz);
+    Tg_out[idx] = Tn;
+    prev = cur;
+    cur = next;
+    idx += ss;
+  };
+  if (s0 + kHeatChunk <= ns) {  // a whole chunk: unrolled, loads issued ahead
+#pragma unroll
+    for (int k = 0; k < kHeatChunk; ++k) cell(s0 + k);
+  } else {
+    for (int s = s0; s < ns; ++s) cell(s);
   }
-  const int64_t idx = (int64_t)(gx + 1) * sx + (int64_t)(gy + 1) * sy + (int64_t)(gz + 1) * sz;
-  const float Tc = __ldg(Tg_in + idx);
-  const float Tn = heat_cell_update(H, Tc, __ldg(Tg_in + idx - sx), __ldg(Tg_in + idx + sx),
-                                    __ldg(Tg_in + idx - sy), __ldg(Tg_in + idx + sy),
-                                    __ldg(Tg_in + idx - sz), __ldg(Tg_in + idx + sz), gx, gy, gz,
-                                    xl, yl, P, dt, Tg_out, idx, sx, sy, sz);
-  Tg_out[idx] = Tn;
 }
 
 }  // namespace pfg
@@ -46,11 +62,13 @@ extern "C" int pfg_heat_step(const pfg_heat_params* h, const float* Tg_in, float
   if (h->layout != PFG_LAYOUT_ZYX && h->layout != PFG_LAYOUT_XYZ) return PFG_ERR_PARAM;
   if (!Tg_in || !Tg_out) return PFG_ERR_NULL;
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  if ((int64_t)(h->nx + 2) * (h->ny + 2) * (h->nz + 2) >= ((int64_t)1 << 31)) return PFG_ERR_SHAPE;
   const HeatConsts H = make_heat_consts(*h);
   const bool xyz = h->layout == PFG_LAYOUT_XYZ;
   const int nf = xyz ? h->nz : h->nx, ns = xyz ? h->nx : h->nz;
-  dim3 block(32, 8, 1);
-  dim3 grid((nf + 31) / 32, (h->ny + 7) / 8, ns);
+  if ((ns + kHeatChunk - 1) / kHeatChunk > 65535) return PFG_ERR_SHAPE;
+  dim3 block(256, 1, 1);
+  dim3 grid((unsigned)((nf * h->ny + 255) / 256), (unsigned)((ns + kHeatChunk - 1) / kHeatChunk), 1);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (xyz)
     heat_step_kernel<true><<<grid, block, 0, s>>>(H, Tg_in, Tg_out, xl, yl, power, dt);
