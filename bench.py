@@ -217,20 +217,24 @@ def time_adjoint():
             "forward_s": t1 - t0, "gradient_s": t2 - t1}
 
 
-def time_heat_step(steps=500):
+def time_heat_step(steps=200, warmup=10, grid=(800, 400, 200)):
     """The standalone explicit heat step (``pfg_heat_step``, the drop-in for
-    ``gamma.update_T``) on the laser-track grid (400 x 200 x 100 interior
-    cells, ghosted float32), both axis orders, ping-pong buffers, CUDA events:
-    microseconds per step and algorithmic bandwidth (read + write 4 bytes per
-    interior cell) against the measured HBM peak."""
+    ``gamma.update_T``) on an 800 x 400 x 200 grid (64M interior cells,
+    ghosted float32: 257 MB per buffer, so the two ping-pong buffers exceed
+    L2), both axis orders, CUDA events: microseconds per step and algorithmic
+    bandwidth (read + write 4 bytes per interior cell) against the measured
+    HBM peak.  ``warmup`` ping-pong pairs (two launches each) precede the
+    timed ``steps`` launches of each axis order."""
     import ctypes
     from jax_am_gb300 import _lib
     from jax_am_gb300.cfd.gamma import make_heat_params
     lib = _lib.load()
     w = WORKLOAD
-    nx, ny, nz = w["Nx"], w["Ny"], w["Nz"]
+    nx, ny, nz = grid
     peak = measured_peak()[0]
-    out = {"workload": f"{nx}x{ny}x{nz} interior cells, 200 W Gaussian, float32"}
+    out = {"workload": f"{nx}x{ny}x{nz} interior cells, 200 W Gaussian, float32",
+           "l2": "inputs larger than L2 (two ghosted buffers of "
+                 f"{(nx + 2) * (ny + 2) * (nz + 2) * 4 / 1e6:.0f} MB)"}
     for name, layout in (("xyz_reference_order", _lib.LAYOUT_XYZ), ("zyx", _lib.LAYOUT_ZYX)):
         shape = (nx + 2, ny + 2, nz + 2) if layout == _lib.LAYOUT_XYZ else (nz + 2, ny + 2, nx + 2)
         a = torch.full(shape, w["T0"], device="cuda")
@@ -241,18 +245,20 @@ def time_heat_step(steps=500):
         def step(src, dst):
             _lib.check(lib.pfg_heat_step(ctypes.byref(h), _lib.ptr(src), _lib.ptr(dst), 50e-6,
                                          100e-6, w["power"], 2e-9, s), "pfg_heat_step")
-        for _ in range(10):
+        for _ in range(warmup):
             step(a, b)
             step(b, a)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        for _ in range(steps // 2):
-            step(a, b)
-            step(b, a)
+        for k in range(steps):
+            if k % 2 == 0:
+                step(a, b)
+            else:
+                step(b, a)
         e1.record()
         torch.cuda.synchronize()
-        us = e0.elapsed_time(e1) / (2 * (steps // 2)) * 1e3
+        us = e0.elapsed_time(e1) / steps * 1e3
         gbs = nx * ny * nz * 8 / (us * 1e-6) / 1e9
         out[name] = {"us_per_step": us, "achieved_GBps": gbs, "roofline_frac": gbs / peak}
         del a, b
@@ -514,8 +520,15 @@ def main():
                     help="eager launches only (warmup then steps), for ncu captures")
     ap.add_argument("--profile-oris", type=int, default=WORKLOAD["num_oris"],
                     help="orientation count of the --profile workload")
+    ap.add_argument("--profile-heat", action="store_true",
+                    help="the standalone heat step only (warmup pairs, then steps launches "
+                         "per axis order), for ncu captures")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.profile_heat:
+        print(json.dumps({"profile_heat": True,
+                          **time_heat_step(steps=args.steps, warmup=args.warmup)}), flush=True)
+        return
     if args.profile_cfd:
         profile_cfd(args)
         return

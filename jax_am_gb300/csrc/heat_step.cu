@@ -7,6 +7,8 @@
 // cells of the unit-stride axis, so loads stay coalesced.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "pfg_device.cuh"
 #include "pfg_host.h"
 
@@ -21,33 +23,44 @@ heat_step_kernel(const __grid_constant__ HeatConsts H, const float* __restrict__
   // fast / middle / slow axis extents (XYZ: z, y, x; ZYX: x, y, z)
   const int nf = XYZ ? H.nz : H.nx, nm = H.ny, ns = XYZ ? H.nx : H.nz;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;  // host keeps nf * nm < 2^31
-  if (t >= nf * nm) return;
+  const bool valid = t < nf * nm;
   const int m = t / nf, f = t - m * nf;
   const int s0 = blockIdx.y * kHeatChunk;
+  // The face-free update runs when no cell of the whole warp's chunk touches a
+  // domain face; the vote keeps that branch warp-uniform (every lane of the
+  // 256-thread block is present at the vote).
+  const bool interior =
+      __all_sync(0xffffffffu, !valid || (f > 0 && f < nf - 1 && m > 0 && m < nm - 1)) &&
+      s0 > 0 && s0 + kHeatChunk < ns;
+  if (!valid) return;
   // ghosted strides: unit along the fast axis (host keeps the ghosted size < 2^31)
   const int sm = nf + 2, ss = (nm + 2) * (nf + 2);
   int idx = (s0 + 1) * ss + (m + 1) * sm + (f + 1);
   float prev = __ldg(Tg_in + idx - ss), cur = __ldg(Tg_in + idx);
-  auto cell = [&](int s) {
+  auto cell = [&](int s, auto faces) {
+    constexpr bool F = decltype(faces)::value;
     const float next = __ldg(Tg_in + idx + ss);
     const float fm = __ldg(Tg_in + idx - 1), fp = __ldg(Tg_in + idx + 1);
     const float mm = __ldg(Tg_in + idx - sm), mp = __ldg(Tg_in + idx + sm);
     const int gx = XYZ ? s : f, gy = m, gz = XYZ ? f : s;
     const int sx = XYZ ? ss : 1, sz = XYZ ? 1 : ss;
-    const float Tn = XYZ ? heat_cell_update(H, cur, prev, next, mm, mp, fm, fp, gx, gy, gz, xl,
-                                            yl, P, dt, Tg_out, idx, sx, sm, sz)
-                         : heat_cell_update(H, cur, fm, fp, mm, mp, prev, next, gx, gy, gz, xl,
-                                            yl, P, dt, Tg_out, idx, sx, sm, sz);
+    const float Tn = XYZ ? heat_cell_update<int, F>(H, cur, prev, next, mm, mp, fm, fp, gx, gy,
+                                                    gz, xl, yl, P, dt, Tg_out, idx, sx, sm, sz)
+                         : heat_cell_update<int, F>(H, cur, fm, fp, mm, mp, prev, next, gx, gy,
+                                                    gz, xl, yl, P, dt, Tg_out, idx, sx, sm, sz);
     Tg_out[idx] = Tn;
     prev = cur;
     cur = next;
     idx += ss;
   };
-  if (s0 + kHeatChunk <= ns) {  // a whole chunk: unrolled, loads issued ahead
+  if (interior) {  // 5 loads, no face tests
 #pragma unroll
-    for (int k = 0; k < kHeatChunk; ++k) cell(s0 + k);
+    for (int k = 0; k < kHeatChunk; ++k) cell(s0 + k, std::false_type{});
+  } else if (s0 + kHeatChunk <= ns) {  // a whole chunk: unrolled, loads issued ahead
+#pragma unroll
+    for (int k = 0; k < kHeatChunk; ++k) cell(s0 + k, std::true_type{});
   } else {
-    for (int s = s0; s < ns; ++s) cell(s);
+    for (int s = s0; s < ns; ++s) cell(s, std::true_type{});
   }
 }
 

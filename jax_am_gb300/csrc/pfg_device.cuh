@@ -228,24 +228,15 @@ __device__ __forceinline__ void laser_at(const pfg_heat_params& hp, double t, fl
   }
 }
 
-// One explicit heat update of interior cell (gx, gy, gz) given its old value
-// and its six old neighbours in the ghosted field (a neighbour across a
-// domain face is the old ghost).  idx is the cell's index in the ghosted
-// array and sx, sy, sz its element strides.  New ghosts of the faces this cell touches
-// are computed from the old ghost and written to Tg_out (gamma.py:18-43);
-// the Laplacian uses them (gamma.py:58-60).  Returns the new interior value.
+// New ghosts of the domain faces that interior cell (gx, gy, gz) touches,
+// computed from the old ghost (gamma.py:18-43), written to Tg_out and
+// substituted for the matching neighbour value.  rk = 1 / k(Tc).
 template <typename IDX>
-__device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc, float Txm,
-                                                  float Txp, float Tym, float Typ, float Tzm,
-                                                  float Tzp, int gx, int gy, int gz, float xl,
-                                                  float yl, float P, float dt, float* Tg_out,
-                                                  IDX idx, IDX sx, IDX sy, IDX sz) {
-  const float k = heat_k(H, Tc);
-  const float rk = rcp_approx(k);
-  const float Tcl = fminf(fmaxf(Tc, H.Ts), H.Tl);
-  const float fl = (Tcl - H.Ts) * H.inv_dTsl;
-  const float cp = 0.2441f * fminf(fmaxf(Tc, 300.f), H.Tl) + 338.39f +
-                   ((fl > 0.f && fl < 1.f) ? H.latent : 0.f);  // gamma.py:12-15
+__device__ __forceinline__ void heat_faces(const HeatConsts& H, float Tc, float rk, float& Txm,
+                                           float& Txp, float& Tym, float& Typ, float& Tzm,
+                                           float& Tzp, int gx, int gy, int gz, float xl,
+                                           float yl, float P, float* Tg_out, IDX idx, IDX sx,
+                                           IDX sy, IDX sz) {
   if (gx == 0) {
     Txm = Tc - heat_robin(H, (Tc + Txm) * 0.5f) * rk * H.dx;
     Tg_out[idx - sx] = Txm;
@@ -276,6 +267,29 @@ __device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc,
     Tzp = Tc - q * rk * H.dz;
     Tg_out[idx + sz] = Tzp;
   }
+}
+
+// One explicit heat update of interior cell (gx, gy, gz) given its old value
+// and its six old neighbours in the ghosted field (a neighbour across a
+// domain face is the old ghost).  idx is the cell's index in the ghosted
+// array and sx, sy, sz its element strides.  New ghosts of the faces this cell touches
+// are computed from the old ghost and written to Tg_out (gamma.py:18-43);
+// the Laplacian uses them (gamma.py:58-60).  Returns the new interior value.
+// FACES = false is for callers that know the cell touches no domain face.
+template <typename IDX, bool FACES = true>
+__device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc, float Txm,
+                                                  float Txp, float Tym, float Typ, float Tzm,
+                                                  float Tzp, int gx, int gy, int gz, float xl,
+                                                  float yl, float P, float dt, float* Tg_out,
+                                                  IDX idx, IDX sx, IDX sy, IDX sz) {
+  const float k = heat_k(H, Tc);
+  const float Tcl = fminf(fmaxf(Tc, H.Ts), H.Tl);
+  const float fl = (Tcl - H.Ts) * H.inv_dTsl;
+  const float cp = 0.2441f * fminf(fmaxf(Tc, 300.f), H.Tl) + 338.39f +
+                   ((fl > 0.f && fl < 1.f) ? H.latent : 0.f);  // gamma.py:12-15
+  if constexpr (FACES)
+    heat_faces(H, Tc, rcp_approx(k), Txm, Txp, Tym, Typ, Tzm, Tzp, gx, gy, gz, xl, yl, P, Tg_out,
+               idx, sx, sy, sz);
   const float txx = (Txm - 2.f * Tc + Txp) * H.rdx2;  // gamma.py:49-51
   const float tyy = (Tym - 2.f * Tc + Typ) * H.rdy2;
   const float tzz = (Tzm - 2.f * Tc + Tzp) * H.rdz2;

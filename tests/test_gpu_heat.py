@@ -48,15 +48,18 @@ def test_update_T_matches_reference_golden(name):
     assert worst <= T_TOL
 
 
-def test_heat_layouts_agree_and_match_oracle():
+@pytest.mark.parametrize("shape", [(19, 13, 7), (50, 20, 50)])
+def test_heat_layouts_agree_and_match_oracle(shape):
     """The kernel on the reference (x-major) layout and on the z-major layout
     gives identical results, equal to the oracle within tolerance; edge and
-    corner ghosts are left untouched."""
+    corner ghosts are left untouched.  At 50 x 20 x 50 whole warps of a
+    chunk touch no domain face (50 cells per row, chunks 8..40 of 50 along the
+    slowest axis), so the face-free path runs beside the face path."""
     from jax_am_gb300 import _lib
     from jax_am_gb300.cfd.gamma import make_heat_params
     import ctypes
     rng = np.random.default_rng(11)
-    nx, ny, nz = 19, 13, 7
+    nx, ny, nz = shape
     dx, dy, dz, dt = 2e-6, 2.5e-6, 1.5e-6, 5e-9
     g = dict(GAMMA_DEFAULTS)
     Tx = f32(rng.uniform(300, 2500, (nx + 2, ny + 2, nz + 2)))
