@@ -17,7 +17,7 @@ namespace pfg {
 constexpr int kHeatChunk = 8;  // cells marched per thread along the slowest axis
 
 template <bool XYZ>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 8)
 heat_step_kernel(const __grid_constant__ HeatConsts H, const float* __restrict__ Tg_in,
                  float* __restrict__ Tg_out, float xl, float yl, float P, float dt) {
   // fast / middle / slow axis extents (XYZ: z, y, x; ZYX: x, y, z)
@@ -53,9 +53,25 @@ heat_step_kernel(const __grid_constant__ HeatConsts H, const float* __restrict__
     cur = next;
     idx += ss;
   };
-  if (interior) {  // 5 loads, no face tests
+  if (interior) {  // 5 loads, no face tests; pointer steps instead of index arithmetic
+    const float* p = Tg_in + idx;
+    float* q = Tg_out + idx;
 #pragma unroll
-    for (int k = 0; k < kHeatChunk; ++k) cell(s0 + k, std::false_type{});
+    for (int k = 0; k < kHeatChunk; ++k) {
+      const float next = __ldg(p + ss);
+      const float fm = __ldg(p - 1), fp = __ldg(p + 1);
+      const float mm = __ldg(p - sm), mp = __ldg(p + sm);
+      const float Tn =
+          XYZ ? heat_cell_update<int, false>(H, cur, prev, next, mm, mp, fm, fp, 0, 0, 0, xl, yl,
+                                             P, dt, Tg_out, 0, 0, 0, 0)
+              : heat_cell_update<int, false>(H, cur, fm, fp, mm, mp, prev, next, 0, 0, 0, xl, yl,
+                                             P, dt, Tg_out, 0, 0, 0, 0);
+      *q = Tn;
+      prev = cur;
+      cur = next;
+      p += ss;
+      q += ss;
+    }
   } else if (s0 + kHeatChunk <= ns) {  // a whole chunk: unrolled, loads issued ahead
 #pragma unroll
     for (int k = 0; k < kHeatChunk; ++k) cell(s0 + k, std::true_type{});

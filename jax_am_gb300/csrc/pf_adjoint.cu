@@ -263,9 +263,7 @@ __device__ __forceinline__ HeatLocal heat_local(const HeatConsts& H, float T) {
   const float Tk = fminf(fmaxf(T, 300.f), H.Tl);
   r.k = 0.0163f * Tk + 4.5847f;
   r.dk = in ? 0.0163f : 0.f;
-  const float Tcl = fminf(fmaxf(T, H.Ts), H.Tl);
-  const float fl = (Tcl - H.Ts) / H.Tl_minus_Ts;
-  r.cp = 0.2441f * Tk + 338.39f + ((fl > 0.f && fl < 1.f) ? H.latent : 0.f);
+  r.cp = 0.2441f * Tk + 338.39f + (heat_mushy(H, T) ? H.latent : 0.f);
   r.dcp = in ? 0.2441f : 0.f;
   r.alpha = r.k / H.rho / r.cp;
   r.dalpha = (r.dk * r.cp - r.k * r.dcp) / (H.rho * r.cp * r.cp);

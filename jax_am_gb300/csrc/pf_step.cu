@@ -335,7 +335,6 @@ HeatConsts make_heat_consts(const pfg_heat_params& h) {
   c.dx2 = h.dx * h.dx; c.dy2 = h.dy * h.dy; c.dz2 = h.dz * h.dz;
   c.rdx2 = 1.f / c.dx2; c.rdy2 = 1.f / c.dy2; c.rdz2 = 1.f / c.dz2;
   c.inv_rho = 1.f / h.rho;
-  c.inv_dTsl = 1.f / (h.Tl - h.Ts);
   c.rho = h.rho;
   c.h = h.h_conv;
   c.sb_eps = (float)((double)h.sigma_sb * (double)h.emissivity);
@@ -343,7 +342,6 @@ HeatConsts make_heat_consts(const pfg_heat_params& h) {
   const float t02 = h.T0 * h.T0;
   c.T0_4 = t02 * t02;
   c.Ts = h.Ts; c.Tl = h.Tl;
-  c.Tl_minus_Ts = h.Tl - h.Ts;
   c.latent = h.latent;
   c.beam_coef = (float)(2.0 * (double)h.absorptivity / 3.14159265358979323846 /
                         ((double)h.beam_radius * (double)h.beam_radius));

@@ -194,8 +194,8 @@ struct HeatConsts {
   float dx, dy, dz;
   float dx2, dy2, dz2;       // d^2
   float rdx2, rdy2, rdz2;    // 1/d^2
-  float inv_rho, inv_dTsl;   // 1/rho, 1/(Tl - Ts)
-  float rho, h, sb_eps, T0, T0_4, Ts, Tl, Tl_minus_Ts, latent;
+  float inv_rho;             // 1/rho
+  float rho, h, sb_eps, T0, T0_4, Ts, Tl, latent;
   float beam_coef;           // 2 * absorptivity / pi / r^2  (times P gives the peak flux)
   float two_over_r2;         // 2 / r^2
   float x_first, y_first;
@@ -203,6 +203,16 @@ struct HeatConsts {
 
 __device__ __forceinline__ float heat_k(const HeatConsts& H, float T) {
   return 0.0163f * fminf(fmaxf(T, 300.f), H.Tl) + 4.5847f;  // gamma.py:14
+}
+
+// Whether the latent heat enters cp (gamma.py:12,15): the liquid fraction
+// fl = (clip(T, Ts, Tl) - Ts) / (Tl - Ts) lies strictly inside (0, 1).  In
+// float32 that is exactly Ts < T < Tl whenever Tl <= 2 Ts (every alloy):
+// clip(T) - Ts is then exact (Sterbenz), and a correctly rounded quotient
+// x / y of floats 0 < x < y is positive and below 1.  For Tl > 2 Ts the two
+// tests can differ only for T within one ulp of Tl.
+__device__ __forceinline__ bool heat_mushy(const HeatConsts& H, float T) {
+  return T > H.Ts && T < H.Tl;
 }
 
 // Robin + radiation flux magnitude h (Tf - T0) + SB eps (Tf^4 - T0^4)
@@ -283,10 +293,8 @@ __device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc,
                                                   float yl, float P, float dt, float* Tg_out,
                                                   IDX idx, IDX sx, IDX sy, IDX sz) {
   const float k = heat_k(H, Tc);
-  const float Tcl = fminf(fmaxf(Tc, H.Ts), H.Tl);
-  const float fl = (Tcl - H.Ts) * H.inv_dTsl;
   const float cp = 0.2441f * fminf(fmaxf(Tc, 300.f), H.Tl) + 338.39f +
-                   ((fl > 0.f && fl < 1.f) ? H.latent : 0.f);  // gamma.py:12-15
+                   (heat_mushy(H, Tc) ? H.latent : 0.f);  // gamma.py:12-15
   if constexpr (FACES)
     heat_faces(H, Tc, rcp_approx(k), Txm, Txp, Tym, Typ, Tzm, Tzp, gx, gy, gz, xl, yl, P, Tg_out,
                idx, sx, sy, sz);

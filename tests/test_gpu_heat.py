@@ -84,6 +84,49 @@ def test_heat_layouts_agree_and_match_oracle(shape):
         np.testing.assert_array_equal(outs[0][sl[0], sl[1], :], Tx[sl[0], sl[1], :])
 
 
+def test_mushy_zone_edges_match_reference_division():
+    """Latent heat enters cp exactly where the reference's float32 liquid
+    fraction (clip(T, Ts, Tl) - Ts) / (Tl - Ts) lies strictly inside (0, 1):
+    cells at Ts, one ulp above Ts, one ulp below Tl and at Tl, each with six
+    neighbours 60 K hotter (a Laplacian large enough that a wrong cp moves
+    the cell by far more than the tolerance), in the face-free interior and
+    next to faces, both axis orders."""
+    from jax_am_gb300 import _lib
+    from jax_am_gb300.cfd.gamma import make_heat_params
+    import ctypes
+    g = dict(GAMMA_DEFAULTS)
+    Ts, Tl = np.float32(g["Ts"]), np.float32(g["Tl"])
+    edges = [Ts, np.nextafter(Ts, np.float32(np.inf)), np.nextafter(Tl, np.float32(0)), Tl]
+    fl = [(np.clip(e, Ts, Tl) - Ts) / (Tl - Ts) for e in edges]  # float32, as the reference
+    assert fl[0] == 0 and 0 < fl[1] and fl[2] < 1 and fl[3] == 1
+    nx, ny, nz = 50, 20, 50
+    dx = dy = dz = 1e-6
+    dt = 2e-9
+    rng = np.random.default_rng(3)
+    Tx = f32(rng.uniform(1540.0, 1650.0, (nx + 2, ny + 2, nz + 2)))
+    cells = [(i, j, k) for i in (1, 25, 50) for j in (1, 10, 20) for k in (1, 25, 50)]
+    for c, (i, j, k) in enumerate(cells):
+        v = edges[c % 4]
+        Tx[i, j, k] = v
+        Tx[i - 1, j, k] = Tx[i, j - 1, k] = Tx[i, j, k - 1] = v + 60.0
+        Tx[i + 1, j, k] = Tx[i, j + 1, k] = Tx[i, j, k + 1] = v + 60.0
+    lib = _lib.load()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    xt, yt = O.cell_centres_top(nx, ny, dx, dy)
+    ref = O.heat_update_T(Tx.astype(np.float64), 1.3e-5, 1.1e-5, xt, yt, 180.0, dx, dy, dz, dt, g)
+    for layout, arr in ((_lib.LAYOUT_XYZ, Tx), (_lib.LAYOUT_ZYX, Tx.transpose(2, 1, 0))):
+        h = make_heat_params(g, nx, ny, nz, dx, dy, dz, layout=layout)
+        tin = torch.tensor(np.ascontiguousarray(arr), dtype=torch.float32, device="cuda")
+        tout = tin.clone()
+        _lib.check(lib.pfg_heat_step(ctypes.byref(h), _lib.ptr(tin), _lib.ptr(tout), 1.3e-5,
+                                     1.1e-5, 180.0, dt, stream), "pfg_heat_step")
+        o = tout.double().cpu().numpy()
+        o = o if layout == _lib.LAYOUT_XYZ else o.transpose(2, 1, 0)
+        for (i, j, k) in cells:
+            assert abs(o[i, j, k] - ref[i, j, k]) <= T_TOL, ((i, j, k), o[i, j, k], ref[i, j, k])
+        assert np.abs(o - ref)[1:-1, 1:-1, 1:-1].max() <= T_TOL
+
+
 def test_uniform_ambient_stays_uniform():
     """With T = T0 everywhere and no beam, the Robin faces give zero flux and
     the field stays exactly at T0."""
