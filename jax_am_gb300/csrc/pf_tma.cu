@@ -20,6 +20,8 @@
 // flight and returns.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include <algorithm>
 #include <cmath>
 
@@ -179,6 +181,7 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   const int xe = min(x0 + P_tx, a.nx), ye = min(y0 + P_ty, a.ny);
   const int zb = zi * a.zc, ze = min(zb + a.zc, a.nz);
   const int txv = xe - x0, tyv = ye - y0;
+  const bool tile_inner = x0 > 0 && xe < a.nx && y0 > 0 && ye < a.ny;
   const int n = P_n;
   const int nplanes = ze - zb + 2;  // planes zb-1 .. ze
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -431,16 +434,23 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
       const float* tc_ = T_s + (size_t)s_cur * P_tslot;
       const float* tn_ = T_s + (size_t)s_next * P_tslot;
       const int zoff = (z + 1) * gsz;
+      auto heat_cells = [&](auto faces) {
+        constexpr bool F = decltype(faces)::value;
 #pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        if (!c_ok[q]) continue;
-        const int o = c_toff[q];
-        const int idx = zoff + c_g[q];
-        const float Tn = heat_cell_update(a.hc, tc_[o], tc_[o - 1], tc_[o + 1], tc_[o - tp],
-                                          tc_[o + tp], tp_[o], tn_[o], c_hx[q], c_hy[q], z, xl, yl,
-                                          Pw, a.dt, a.T_out, idx, 1, gsy, gsz);
-        a.T_out[idx] = Tn;
-      }
+        for (int q = 0; q < 2; ++q) {
+          if (!c_ok[q]) continue;
+          const int o = c_toff[q];
+          const int idx = zoff + c_g[q];
+          const float Tn = heat_cell_update<int, F>(a.hc, tc_[o], tc_[o - 1], tc_[o + 1],
+                                                    tc_[o - tp], tc_[o + tp], tp_[o], tn_[o],
+                                                    c_hx[q], c_hy[q], z, xl, yl, Pw, a.dt,
+                                                    a.T_out, idx, 1, gsy, gsz);
+          a.T_out[idx] = Tn;
+        }
+      };
+      // CTA-uniform: no cell of this tile plane touches a domain face
+      if (tile_inner && z > 0 && z < a.nz - 1) heat_cells(std::false_type{});
+      else heat_cells(std::true_type{});
     }
     if (z + 1 < ze) cell_coefs(s_next, (m + 1) & 1, z + 1);
 

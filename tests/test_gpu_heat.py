@@ -48,13 +48,14 @@ def test_update_T_matches_reference_golden(name):
     assert worst <= T_TOL
 
 
-@pytest.mark.parametrize("shape", [(19, 13, 7), (50, 20, 50)])
+@pytest.mark.parametrize("shape", [(19, 13, 7), (50, 20, 50), (400, 200, 100)])
 def test_heat_layouts_agree_and_match_oracle(shape):
     """The kernel on the reference (x-major) layout and on the z-major layout
     gives identical results, equal to the oracle within tolerance; edge and
     corner ghosts are left untouched.  At 50 x 20 x 50 whole warps of a
     chunk touch no domain face (50 cells per row, chunks 8..40 of 50 along the
-    slowest axis), so the face-free path runs beside the face path."""
+    slowest axis), so the face-free path runs beside the face path; 400 x 200
+    x 100 is the laser-track grid (8M cells, 61-74 % face-free warps)."""
     from jax_am_gb300 import _lib
     from jax_am_gb300.cfd.gamma import make_heat_params
     import ctypes
