@@ -263,31 +263,73 @@ pf_diag_kernel(const __grid_constant__ DiagArgs a) {
   }
 }
 
-__global__ void __launch_bounds__(256)
+// Folds the per-block partial records in a fixed order, so the result is
+// bit-reproducible.  Scalars: thread t folds records t, t + 256 in order, then
+// a fixed binary tree over the 256 threads.  Masses: thread (g, i) of
+// G = 256 / n groups folds records g, g + G, ... of orientation i in order,
+// then thread i folds the G group sums in order.  Every chain is short, so
+// the slow float64 pipe and the load latency are paid a few dozen times, not
+// once per record.
+constexpr int kFinishThreads = 256;
+
+__device__ __forceinline__ double nan_max(double a, double b) {
+  return isnan(a) ? a : (isnan(b) ? b : (b > a ? b : a));
+}
+
+__global__ void __launch_bounds__(kFinishThreads)
 pf_diag_finish_kernel(const DiagPartial* __restrict__ parts, int nparts, int n, long long ncell,
                       pfg_diag* __restrict__ out) {
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    double m = 0.0;
-    for (int b = 0; b < nparts; ++b) m += parts[b].mass[i];
-    out->mass[i] = m;
+  __shared__ double s_en[kFinishThreads], s_mt[kFinishThreads];
+  __shared__ long long s_cnt[kFinishThreads][3];
+  __shared__ double s_mass[kFinishThreads];  // [group][orientation], G * n <= 256
+  const int t = threadIdx.x;
+  double en = 0.0, mt = -INFINITY;
+  long long c0 = 0, c1 = 0, c2 = 0;
+  for (int b = t; b < nparts; b += kFinishThreads) {
+    const DiagPartial& p = parts[b];
+    en += p.energy;
+    mt = nan_max(mt, p.max_T);
+    c0 += p.changed;
+    c1 += p.liquid;
+    c2 += p.nonfinite;
   }
-  for (int i = n + threadIdx.x; i < PFG_MAX_ORIS; i += blockDim.x) out->mass[i] = 0.0;
-  if (threadIdx.x == 0) {
-    double en = 0.0, mt = -INFINITY;
-    long long c0 = 0, c1 = 0, c2 = 0;
-    for (int b = 0; b < nparts; ++b) {
-      en += parts[b].energy;
-      if (parts[b].max_T > mt || isnan(parts[b].max_T)) mt = isnan(mt) ? mt : parts[b].max_T;
-      c0 += parts[b].changed;
-      c1 += parts[b].liquid;
-      c2 += parts[b].nonfinite;
+  s_en[t] = en;
+  s_mt[t] = mt;
+  s_cnt[t][0] = c0;
+  s_cnt[t][1] = c1;
+  s_cnt[t][2] = c2;
+  const int G = kFinishThreads / n;  // n <= 64: at least 4 groups
+  if (t < G * n) {
+    const int g = t / n, i = t - g * n;
+    double m = 0.0;
+#pragma unroll 8
+    for (int b = g; b < nparts; b += G) m += parts[b].mass[i];
+    s_mass[t] = m;
+  }
+  __syncthreads();
+  for (int half = kFinishThreads / 2; half > 0; half >>= 1) {
+    if (t < half) {
+      s_en[t] += s_en[t + half];
+      s_mt[t] = nan_max(s_mt[t], s_mt[t + half]);
+      s_cnt[t][0] += s_cnt[t + half][0];
+      s_cnt[t][1] += s_cnt[t + half][1];
+      s_cnt[t][2] += s_cnt[t + half][2];
     }
-    out->energy = en;
-    out->max_T = mt;
+    __syncthreads();
+  }
+  if (t < n) {
+    double m = 0.0;
+    for (int g = 0; g < G; ++g) m += s_mass[g * n + t];
+    out->mass[t] = m;
+  }
+  for (int i = n + t; i < PFG_MAX_ORIS; i += kFinishThreads) out->mass[i] = 0.0;
+  if (t == 0) {
+    out->energy = s_en[0];
+    out->max_T = s_mt[0];
     out->n_cells = ncell;
-    out->n_ori_changed = c0;
-    out->n_liquid = c1;
-    out->n_nonfinite = c2;
+    out->n_ori_changed = s_cnt[0][0];
+    out->n_liquid = s_cnt[0][1];
+    out->n_nonfinite = s_cnt[0][2];
   }
 }
 
@@ -314,61 +356,108 @@ static void launch_diag_g(const DiagArgs& a, int nb, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // The metrics of the reference's inspect_sol only (argmax changes, liquid
 // cells, max T, non-finite values).  With no per-orientation sums to keep,
-// one thread takes a whole cell: its orientations are read as 16-byte
-// vectors (several in flight per thread) and scanned in order, so the argmax
-// needs no shuffles.  Partial records as for pf_diag_kernel, with zero energy
-// and mass.
+// one lane takes a whole cell and scans its orientations in order, so the
+// argmax needs no shuffles.  A warp works on 32 consecutive cells at a time:
+// their 32 n floats are contiguous in eta, so the warp first copies them to
+// its own shared-memory slice with fully coalesced 16-byte loads (every load
+// instruction moves 512 contiguous bytes), then each lane reads its cell from
+// shared memory (a cell of n = 20 floats is 5 vectors: an odd stride, so the
+// reads are free of bank conflicts).  Partial records as for pf_diag_kernel,
+// with zero energy and mass.
 // ---------------------------------------------------------------------------
+// Up to 32 warps per block, two blocks per SM: the chunk loads of 64 warps
+// per SM in flight, as the blocks are capped at the partial-record count.
+constexpr int kInspectMaxWarps = 32;
+constexpr int kInspectSmemBudget = 100 * 1024;  // per block, opted in above 48 KB
+
+// warps of an inspect block: as many as keep 32 cells per warp, plus the
+// kernel's static shared memory, within kInspectSmemBudget
+static int inspect_warps(int n) {
+  const int w = (kInspectSmemBudget - 2048) / (32 * 4 * n);
+  return w < kInspectMaxWarps ? (w < 1 ? 1 : w) : kInspectMaxWarps;
+}
+
 template <bool VEC4>
-__global__ void __launch_bounds__(kDiagThreads) pf_inspect_kernel(const __grid_constant__ DiagArgs a) {
-  constexpr int kWarps = kDiagThreads / 32;
+__global__ void __launch_bounds__(32 * kInspectMaxWarps)
+pf_inspect_kernel(const __grid_constant__ DiagArgs a) {
+  extern __shared__ float4 s_cells[];  // per warp: 32 cells of n floats
+  constexpr int kWarps = kInspectMaxWarps;
   __shared__ double s_maxT[kWarps];
   __shared__ long long s_cnt[kWarps][3];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int n = a.n;
-  const int64_t ncell = (int64_t)a.nx * a.ny * a.nz;
-  const int64_t xy = (int64_t)a.nx * a.ny;
+  const int ncell = a.nx * a.ny * a.nz;  // < 2^31 (host checks)
+  const int xy = a.nx * a.ny;
   const int64_t gsy = a.nx + 2, gsz = (int64_t)(a.ny + 2) * (a.nx + 2);
+  float* ws = reinterpret_cast<float*>(s_cells) + (size_t)warp * 32 * n;
   float maxT = -INFINITY;
   int changed = 0, liquid = 0, nonfinite = 0;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    int64_t ti = c;
-    if (a.T_ghosted) {
-      const int64_t z = c / xy, r = c - z * xy, y = r / a.nx, x = r - y * a.nx;
-      ti = (z + 1) * gsz + (y + 1) * gsy + x + 1;
+  const int nchunks = (int)(((int64_t)ncell + 31) / 32);
+  for (int ch = blockIdx.x * nwarps + warp; ch < nchunks; ch += gridDim.x * nwarps) {
+    const int c0 = ch * 32;
+    const int cells = min(32, ncell - c0);
+    // the lane's T is loaded together with the chunk, not after it
+    float T = 0.f;
+    if (lane < cells) {
+      const int c = c0 + lane;
+      int64_t ti = c;
+      if (a.T_ghosted) {
+        const int z = c / xy, r = c - z * xy, y = r / a.nx, x = r - y * a.nx;
+        ti = (int64_t)(z + 1) * gsz + (int64_t)(y + 1) * gsy + x + 1;
+      }
+      T = __ldg(a.T + ti);
     }
-    const float T = a.T[ti];
-    const int a0 = a.argmax0 ? a.argmax0[c] : 0;
-    const float* e = a.eta + c * n;
-    float best = -INFINITY;
-    int bi = 1 << 30;
     if constexpr (VEC4) {
-      const float4* e4 = reinterpret_cast<const float4*>(e);
+      const float4* src = reinterpret_cast<const float4*>(a.eta + (int64_t)c0 * n);
+      float4* dst = reinterpret_cast<float4*>(ws);
+      const int tot = cells * (n >> 2);
 #pragma unroll 4
-      for (int k = 0; k < n / 4; ++k) {
-        const float4 u = __ldg(e4 + k);
-        auto visit = [&](float q, int i) {
+      for (int j = lane; j < tot; j += 32) dst[j] = __ldg(src + j);
+    } else {
+      const float* src = a.eta + (int64_t)c0 * n;
+      const int tot = cells * n;
+#pragma unroll 4
+      for (int j = lane; j < tot; j += 32) ws[j] = __ldg(src + j);
+    }
+    __syncwarp();
+    if (lane < cells) {
+      const int c = c0 + lane;
+      const float* e = ws + lane * n;
+      // Fast scan: the first maximum by strict '>' (exact for finite values),
+      // and bad = sum of q * 0, which turns NaN at any NaN or infinity.
+      float best = -INFINITY, bad = 0.f;
+      int bi = 0;
+      auto fast = [&](float q, int i) {
+        bad = fmaf(q, 0.f, bad);
+        if (q > best) { best = q; bi = i; }
+      };
+      if constexpr (VEC4) {
+        const float4* e4 = reinterpret_cast<const float4*>(e);
+        for (int k = 0; k < (n >> 2); ++k) {
+          const float4 u = e4[k];
+          fast(u.x, 4 * k);
+          fast(u.y, 4 * k + 1);
+          fast(u.z, 4 * k + 2);
+          fast(u.w, 4 * k + 3);
+        }
+      } else {
+        for (int i = 0; i < n; ++i) fast(e[i], i);
+      }
+      if (isnan(bad)) {  // a non-finite value: np.argmax's rules (first NaN wins) and the count
+        best = -INFINITY;
+        bi = 1 << 30;
+        for (int i = 0; i < n; ++i) {
+          const float q = e[i];
           if (!isfinite(q)) ++nonfinite;
           if (argmax_better(q, i, best, bi)) { best = q; bi = i; }
-        };
-        visit(u.x, 4 * k);
-        visit(u.y, 4 * k + 1);
-        visit(u.z, 4 * k + 2);
-        visit(u.w, 4 * k + 3);
+        }
       }
-    } else {
-#pragma unroll 4
-      for (int i = 0; i < n; ++i) {
-        const float q = __ldg(e + i);
-        if (!isfinite(q)) ++nonfinite;
-        if (argmax_better(q, i, best, bi)) { best = q; bi = i; }
-      }
+      if (T >= a.tl_ge) ++liquid;
+      if (T > maxT || isnan(T)) maxT = isnan(maxT) ? maxT : T;
+      if (a.argmax_out) a.argmax_out[c] = bi;
+      if (a.argmax0 && __ldg(a.argmax0 + c) != bi) ++changed;
     }
-    if (T >= a.tl_ge) ++liquid;
-    if (T > maxT || isnan(T)) maxT = isnan(maxT) ? maxT : T;
-    if (a.argmax_out) a.argmax_out[c] = bi;
-    if (a.argmax0 && a0 != bi) ++changed;
+    __syncwarp();  // the slice is rewritten by the next chunk
   }
   double mt = (double)maxT;
   long long c0 = changed, c1 = liquid, c2 = nonfinite;
@@ -392,7 +481,7 @@ __global__ void __launch_bounds__(kDiagThreads) pf_inspect_kernel(const __grid_c
   if (threadIdx.x == 0) {
     double t2 = -INFINITY;
     long long d0 = 0, d1 = 0, d2 = 0;
-    for (int w = 0; w < kWarps; ++w) {
+    for (int w = 0; w < nwarps; ++w) {
       if (s_maxT[w] > t2 || isnan(s_maxT[w])) t2 = isnan(t2) ? t2 : s_maxT[w];
       d0 += s_cnt[w][0];
       d1 += s_cnt[w][1];
@@ -429,10 +518,24 @@ int launch_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_
   }
   a.eta = eta; a.T = T; a.argmax0 = argmax0; a.argmax_out = argmax_out;
   a.partials = static_cast<DiagPartial*>(scratch);
-  const int nb = diag_blocks(*p);
+  int nb = diag_blocks(*p);
   if (!full) {
-    if (a.n % 4 == 0) pf_inspect_kernel<true><<<nb, kDiagThreads, 0, s>>>(a);
-    else pf_inspect_kernel<false><<<nb, kDiagThreads, 0, s>>>(a);
+    // no more blocks than partial records in the scratch (diag_blocks) or
+    // than chunks of 32 cells per warp
+    const int w = inspect_warps(a.n);
+    const long long nchunks = ((long long)a.nx * a.ny * a.nz + 31) / 32;
+    const long long need = (nchunks + w - 1) / w;
+    nb = (int)(need < nb ? (need < 1 ? 1 : need) : nb);
+    const size_t smem = (size_t)w * 32 * a.n * sizeof(float);
+    const void* fn = (a.n % 4 == 0) ? (const void*)pf_inspect_kernel<true>
+                                    : (const void*)pf_inspect_kernel<false>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)smem);
+      if (e != cudaSuccess) return record_cuda(e);
+    }
+    if (a.n % 4 == 0) pf_inspect_kernel<true><<<nb, 32 * w, smem, s>>>(a);
+    else pf_inspect_kernel<false><<<nb, 32 * w, smem, s>>>(a);
   } else switch (diag_group(a.n)) {
     case 1: launch_diag_g<1>(a, nb, s); break;
     case 2: launch_diag_g<2>(a, nb, s); break;
@@ -442,7 +545,7 @@ int launch_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return record_cuda(e);
-  pf_diag_finish_kernel<<<1, 256, 0, s>>>(a.partials, nb, p->num_oris,
+  pf_diag_finish_kernel<<<1, kFinishThreads, 0, s>>>(a.partials, nb, p->num_oris,
                                           (long long)p->nx * p->ny * p->nz, out);
   return record_cuda(cudaGetLastError());
 }

@@ -247,7 +247,8 @@ class PFSolver:
     def argmax(self, eta):
         """First-maximum orientation index per cell (int32), from the diagnostics kernel."""
         out = torch.empty(self.N, dtype=torch.int32, device="cuda")
-        self._diag(eta, torch.zeros(self.N, device="cuda"), None, out, ghosted=False)
+        self._diag(eta, torch.zeros(self.N, device="cuda"), None, out, ghosted=False,
+                   entry="pfg_pf_inspect")
         return out
 
     def _diag_launch(self, eta, T, argmax0, argmax_out, ghosted, entry):

@@ -59,21 +59,45 @@ def test_inspect_sol_raises_on_nan(capsys):
 
 
 @pytest.mark.parametrize("shape,n,bc", [((17, 13, 6), 20, "periodic"), ((9, 7, 5), 5, None),
-                                        ((64, 48, 40), 12, None)])
+                                        ((64, 48, 40), 12, None), ((4, 4, 4), 33, None),
+                                        ((31, 2, 3), 64, None), ((50, 40, 30), 7, "periodic"),
+                                        ((2, 1, 1), 1, None), ((100, 50, 25), 20, None)])
 def test_inspect_matches_full_diagnostics(shape, n, bc):
     """pfg_pf_inspect (the inspect_sol metrics only) gives the same counts,
-    max T and argmax map as the full reduction, and zero energy and mass."""
+    max T and argmax map as the full reduction, and zero energy and mass:
+    with first-maximum ties, an all-zero cell, NaN and Inf values, partial
+    last chunks of 32 cells and n from 1 to 64."""
     from jax_am_gb300.phase_field.allen_cahn import PFSolver
     poly, eta, T, pf_args, oargs, obc = pf_case(shape, n, 0.0, seed=5, bc=bc)
     s = PFSolver(pf_args, poly)
     eta0 = np.roll(eta, 1, axis=1)
+    N = len(eta)
+    ties = np.zeros(n, dtype=eta.dtype)
+    ties[[0, n - 1]] = 0.7
+    eta[0] = ties
+    if N > 1:
+        eta[1] = 0.0
+    if N > 2:
+        eta[N - 1, n // 2] = np.nan  # NaN wins the argmax
+        eta[N // 2, 0] = np.inf
     full = s.diagnostics(eta, T, eta0)
     light = s.inspect(eta, T, eta0)
     for key in ("n_ori_changed", "n_liquid", "n_nonfinite", "max_T", "n_cells"):
         assert light[key] == full[key], key
+    assert light["n_nonfinite"] == (2 if N > 2 else 0)
     assert light["energy"] == 0.0 and not np.any(light["mass"])
     m = O.inspect(eta, eta0, T, oargs["T_liquidus"])
     assert light["pct_liquid"] == pytest.approx(m["pct_liquid"], abs=1e-12)
+    # argmax maps of both kernels, and numpy's (NaN first, then first maximum)
+    ed = torch.tensor(eta, dtype=torch.float32, device="cuda")
+    Td = torch.tensor(np.asarray(T, dtype=np.float32).reshape(-1), device="cuda")
+    maps = []
+    for entry in ("pfg_pf_diag", "pfg_pf_inspect"):
+        am = torch.empty(N, dtype=torch.int32, device="cuda")
+        s._diag(ed, Td, None, am, False, entry)
+        maps.append(am.cpu().numpy())
+    np.testing.assert_array_equal(maps[0], maps[1])
+    np.testing.assert_array_equal(maps[1], np.argmax(eta.astype(np.float32), axis=1))
 
 
 def test_inspect_async_is_ordered_before_later_steps():
