@@ -265,6 +265,33 @@ def time_heat_step(steps=200, warmup=10, grid=(800, 400, 200)):
     return out
 
 
+def time_inspect(solver, run, reps=50):
+    """The reference's inspect_sol metrics on the laser-track state
+    (``PFSolver.inspect``'s kernels: argmax changes, liquid cells, max T,
+    non-finite values, one pass over eta and T) and the full diagnostics
+    (energy and per-orientation mass as well), CUDA events over ``reps``
+    back-to-back launches: microseconds per record and the bandwidth of the
+    inspect pass (eta + ghosted T read once) against the measured HBM peak."""
+    eta, T = run.state, run.T_ghosted
+
+    def timed(entry):
+        for _ in range(3):
+            solver._diag_launch(eta, T, None, None, True, entry)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            solver._diag_launch(eta, T, None, None, True, entry)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps * 1e3
+    us = timed("pfg_pf_inspect")
+    gbs = (eta.numel() + T.numel()) * 4 / (us * 1e-6) / 1e9
+    return {"workload": "laser_track_8M state (400x200x100 cells, n=20), ghosted T",
+            "inspect_us": us, "achieved_GBps": gbs, "roofline_frac": gbs / measured_peak()[0],
+            "full_diag_us": timed("pfg_pf_diag")}
+
+
 def time_cfd(steps=20, warmup=3, cpu=False):
     """The implicit CFD solver (``AM_3d``, float64) on the reference's
     standalone CFD driver configuration (``workloads.cfd_simple_case``):
@@ -520,12 +547,26 @@ def main():
                     help="eager launches only (warmup then steps), for ncu captures")
     ap.add_argument("--profile-oris", type=int, default=WORKLOAD["num_oris"],
                     help="orientation count of the --profile workload")
+    ap.add_argument("--profile-inspect", action="store_true",
+                    help="the inspect_sol metrics kernels only, on the laser-track state "
+                         "after --warmup steps (50 timed records each), for ncu captures")
     ap.add_argument("--profile-heat", action="store_true",
                     help="the standalone heat step only (warmup pairs, then steps launches "
                          "per axis order), for ncu captures")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.profile_inspect:
+        import __graft_entry__
+        __graft_entry__.build()
+        from jax_am_gb300.runner import HeatPFRun
+        solver, g, path, _ = build_case(WORKLOAD)
+        run = HeatPFRun(solver, g, path)
+        run.run(args.warmup, graph=False)
+        print(json.dumps({"profile_inspect": True, **time_inspect(solver, run)}), flush=True)
+        return
     if args.profile_heat:
+        import __graft_entry__
+        __graft_entry__.build()
         print(json.dumps({"profile_heat": True,
                           **time_heat_step(steps=args.steps, warmup=args.warmup)}), flush=True)
         return
@@ -593,6 +634,9 @@ def main():
                 "measured" else "fallback 6.8 TB/s", "kernel": KERNEL,
                 "algorithmic_bytes_per_launch": bytes_step}
 
+    # the inspect_sol metrics on the state just reached (the pass e2e runs every 20 steps)
+    inspect = time_inspect(solver, run) if rank == 0 else None
+
     # end to end through the public API with host buffers
     e2e = None
     if not args.no_e2e:
@@ -631,7 +675,7 @@ def main():
             "gpu_launches": gpu_launches, "clocks": clocks,
             "plan": _lib.describe_plan(solver.params),
             "serving": serving, "adjoint": adjoint, "other_configs": others,
-            "cfd_am3d": cfd, "heat_step": heat,
+            "cfd_am3d": cfd, "heat_step": heat, "inspect": inspect,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

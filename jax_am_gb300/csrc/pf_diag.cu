@@ -378,7 +378,7 @@ static int inspect_warps(int n) {
 }
 
 template <bool VEC4>
-__global__ void __launch_bounds__(32 * kInspectMaxWarps)
+__global__ void __launch_bounds__(32 * kInspectMaxWarps, 2)
 pf_inspect_kernel(const __grid_constant__ DiagArgs a) {
   extern __shared__ float4 s_cells[];  // per warp: 32 cells of n floats
   constexpr int kWarps = kInspectMaxWarps;
