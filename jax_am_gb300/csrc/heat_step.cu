@@ -1,10 +1,12 @@
 // Explicit finite-difference heat step on the ghosted field (jax_am/cfd/gamma.py:55-61).
-// A thread owns one (fast, middle) position and marches CH cells along the
-// slowest axis, keeping the previous, current and next values of that axis in
-// registers: per cell it loads the next value and the four in-plane
+// A thread owns one (fast, middle) position and marches kHeatChunk cells along
+// the slowest axis, keeping the previous, current and next values of that axis
+// in registers: per cell it loads the next value and the four in-plane
 // neighbours (a neighbour across a face is the previous ghost value).  The
 // field may be in either axis order; consecutive threads take consecutive
-// cells of the unit-stride axis, so loads stay coalesced.
+// cells of the unit-stride axis, so loads stay coalesced.  A warp whose whole
+// chunk touches no domain face runs the update with the face code compiled
+// out and steps pointers instead of recomputing indices.
 #include <cuda_runtime.h>
 
 #include <type_traits>
