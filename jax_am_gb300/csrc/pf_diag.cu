@@ -424,7 +424,8 @@ pf_inspect_kernel(const __grid_constant__ DiagArgs a) {
       const int c = c0 + lane;
       const float* e = ws + lane * n;
       // Fast scan: the first maximum by strict '>' (exact for finite values),
-      // and bad = sum of q * 0, which turns NaN at any NaN or infinity.
+      // and bad = sum of q * 0, which turns NaN at any NaN or infinity (the
+      // library is built without fast-math, so q * 0 is not folded to 0).
       float best = -INFINITY, bad = 0.f;
       int bi = 0;
       auto fast = [&](float q, int i) {
