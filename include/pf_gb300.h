@@ -295,6 +295,28 @@ int pfg_heat_pf_step(const pfg_pf_params* p, const pfg_heat_params* h,
                      const pfg_clock* clk_in, pfg_clock* clk_out,
                      float dt, void* stream);
 
+/* The same fused step with a compensated temperature: the ghosted field is
+ * held as two float32 arrays whose sum is the temperature (Tg + Tlo, |Tlo|
+ * at most half an ulp of Tg; start from Tlo = 0), and the heat update is
+ * evaluated in double-float arithmetic (pairs of float32) wherever the
+ * temperature is far from ambient and on every domain face.  A float32
+ * temperature rounds to ~1e-3 K per step at 1e4 K and drifts from a
+ * float64 run by ~1e-2 K over 2000 steps of the laser-track workload; the
+ * compensated one stays within ~1e-5 K.  The phase field reads Tg.
+ * Available for the cell-per-lane kernel (num_oris = 20, see
+ * pfg_heat_pf_step_comp_supported); otherwise PFG_ERR_PARAM.  Tg_in/Tg_out
+ * and Tlo_in/Tlo_out must not alias.  Same reference functions as
+ * pfg_heat_pf_step (allen_cahn.py:106-114, gamma.py:9-61). */
+int pfg_heat_pf_step_comp(const pfg_pf_params* p, const pfg_heat_params* h,
+                          const float* eta_in, float* eta_out,
+                          const float* Tg_in, const float* Tlo_in,
+                          float* Tg_out, float* Tlo_out,
+                          const pfg_clock* clk_in, pfg_clock* clk_out,
+                          float dt, void* stream);
+/* 1 if pfg_heat_pf_step_comp runs for these parameters on the current
+ * device, 0 if not; a negative value is -pfg_status. */
+int pfg_heat_pf_step_comp_supported(const pfg_pf_params* p);
+
 /* ---- batched serving ------------------------------------------------------
  * Many independent directional-solidification solves (each with its own
  * grid, orientation count, parameters and step count) advanced together: one
@@ -429,7 +451,10 @@ int pfg_pf_inspect(const pfg_pf_params* p, const float* eta, const float* T, int
  * the library holds until the process exits.
  *  - The first call on a device looks up the array's device address
  *    (cudaGetSymbolAddress) with that device current; make that first call
- *    before any stream capture.
+ *    before any stream capture.  The address is kept for the life of the
+ *    process, so do not reset the device (cudaDeviceReset, or a reset of
+ *    its primary context) while the library is loaded: the array would move
+ *    and the kept address would point at freed memory.
  *  - Every call on a device shares the one array: calls whose work overlaps
  *    on the GPU (different streams, no ordering between them) race and give
  *    wrong results.  Order them on one stream or with events.

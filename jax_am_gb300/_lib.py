@@ -144,6 +144,9 @@ _PROTOS = {
     "pfg_heat_step": (_I, [ctypes.POINTER(HeatParams), _P, _P, _F, _F, _F, _F, _P]),
     "pfg_heat_pf_step": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(HeatParams), _P, _P, _P,
                               _P, _P, _P, _F, _P]),
+    "pfg_heat_pf_step_comp": (_I, [ctypes.POINTER(PfParams), ctypes.POINTER(HeatParams), _P, _P,
+                                   _P, _P, _P, _P, _P, _P, _F, _P]),
+    "pfg_heat_pf_step_comp_supported": (_I, [ctypes.POINTER(PfParams)]),
     "pfg_batch_table_bytes": (ctypes.c_int64, [_I]),
     "pfg_batch_encode": (_I, [ctypes.POINTER(BatchJob), _I, _P, ctypes.c_int64,
                               ctypes.POINTER(ctypes.c_int64)]),

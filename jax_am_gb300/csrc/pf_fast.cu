@@ -48,7 +48,9 @@ extern int g_tma_consumers;
 extern int g_cfd_cells_per_thread;
 extern int g_fixed_plans;
 // Plan overrides for tuning sweeps (0 = automatic).
-static int g_tune_wx = 0, g_tune_rpw = 0, g_tune_stages = 0, g_tune_zchunks = 0;
+static int g_tune_wx = 0, g_tune_rpw = 0, g_tune_stages = 0;
+int g_tune_zchunks = 0;  // pfg_tune key 3 (every z-marching planner)
+long long g_probe_wait = 0;  // pfg_tune key 8: cycles of the wait probe, 0 = off
 
 int set_tune(int key, int value) {
   if (value < 0) return PFG_ERR_PARAM;
@@ -67,6 +69,7 @@ int set_tune(int key, int value) {
             g_cfd_cells_per_thread = value ? value : 4; return PFG_OK;
     case 7: if (value > 1) return PFG_ERR_PARAM;
             g_fixed_plans = value ? 0 : 1; return PFG_OK;
+    case 8: g_probe_wait = value; return PFG_OK;
     default: return PFG_ERR_PARAM;
   }
 }

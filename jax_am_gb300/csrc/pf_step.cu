@@ -351,6 +351,35 @@ HeatConsts make_heat_consts(const pfg_heat_params& h) {
   return c;
 }
 
+static DF df_split(double v) {
+  const float h = (float)v;
+  return DF{h, (float)(v - (double)h)};
+}
+
+// The DF constants of the compensated heat update, from the float32
+// parameters (so the device evaluates exactly the model those values
+// define) and the reference's literal coefficients (gamma.py:12-15).
+HeatDF make_heat_df(const pfg_heat_params& h, float dt) {
+  HeatDF d;
+  d.k1 = df_split(0.0163);
+  d.k0 = df_split(4.5847);
+  d.c1 = df_split(0.2441);
+  d.c0 = df_split(338.39);
+  d.latent = df_split((double)h.latent);
+  const double r = (double)h.beam_radius;
+  d.beam_coef = df_split(2.0 * (double)h.absorptivity / 3.14159265358979323846 / (r * r));
+  d.two_over_r2 = df_split(2.0 / (r * r));
+  d.sb_eps = df_split((double)h.sigma_sb * (double)h.emissivity);
+  const double t0 = (double)h.T0;
+  d.T0_4 = df_split(t0 * t0 * t0 * t0);
+  d.rd2[0] = df_split(1.0 / ((double)h.dx * (double)h.dx));
+  d.rd2[1] = df_split(1.0 / ((double)h.dy * (double)h.dy));
+  d.rd2[2] = df_split(1.0 / ((double)h.dz * (double)h.dz));
+  d.dt = DF{dt, 0.f};
+  d.hot = h.T0 + 50.f;
+  return d;
+}
+
 int vec_width(int n) { return (n % 4 == 0) ? 4 : (n % 2 == 0) ? 2 : 1; }
 
 TilePlan plan_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
@@ -433,6 +462,7 @@ void fill_step_args(StepArgs& a, const pfg_pf_params& p, const TilePlan& t, floa
   a.tslot = t.tslot; a.tpc = t.tpc; a.rs = t.rs;
   a.tiles_x = t.tiles_x; a.tiles_y = t.tiles_y; a.zchunks = t.zchunks;
   a.h_z = p.h_z;
+  a.probe_wait = g_probe_wait;
   for (int i = 0; i < 3 * p.num_oris * 3; ++i) a.dirs[i] = p.grain_dirs[i];
 }
 
@@ -466,13 +496,25 @@ TilePlan plan_for_current_device(const pfg_pf_params& p) {
   return plan_tiles(p.nx, p.ny, p.nz, p.num_oris, d.sm_count, d.smem_per_sm, d.smem_per_block);
 }
 
-// Plan and launch one step: the warp-per-cells kernel when the orientation
+static bool plan_lane(const pfg_pf_params& p, TilePlan* t) {
+  const DeviceInfo& d = device_info();
+  return plan_lane_tiles(p.nx, p.ny, p.nz, p.num_oris, d.sm_count, d.smem_per_sm,
+                         d.smem_per_block, g_tune_zchunks, t);
+}
+
+// Plan and launch one step: the cell-per-lane kernel (num_oris = 20), else
+// the TMA-fed kernel, else the warp-per-cells kernel when the orientation
 // count allows it (num_oris / VEC <= 32), otherwise the generic kernel.
 template <int TSRC>
 static cudaError_t dispatch(StepArgs& a, const pfg_pf_params& p, float dt, cudaStream_t s) {
   const DeviceInfo& d = device_info();
   TilePlan t;
   const int v = g_kernel_variant;
+  if (v == 0 && plan_lane(p, &t)) {
+    fill_common(a, p, t, dt);
+    a.cpw = t.cpw; a.wx = t.wx; a.rpw = t.rpw;
+    return launch_lane_kernel<TSRC>(a, t, s);
+  }
   if ((v == 0 || v == 3) &&
       plan_tma_tiles(p.nx, p.ny, p.nz, p.num_oris, p.bc_x, d.sm_count, d.smem_per_sm, &t)) {
     fill_common(a, p, t, dt);
@@ -505,7 +547,9 @@ extern "C" int pfg_describe_plan(const pfg_pf_params* p, int32_t* out) {
   TilePlan t;
   int kernel;
   const int variant = g_kernel_variant;
-  if ((variant == 0 || variant == 3) &&
+  if (variant == 0 && plan_lane(*p, &t)) {
+    kernel = 4;
+  } else if ((variant == 0 || variant == 3) &&
       plan_tma_tiles(p->nx, p->ny, p->nz, p->num_oris, p->bc_x, d.sm_count, d.smem_per_sm, &t)) {
     kernel = 3;
   } else if ((variant == 0 || variant == 2 || variant == 3) &&
@@ -529,6 +573,7 @@ extern "C" int pfg_fixed_plan(const pfg_pf_params* p) {
   const DeviceInfo& d = device_info();
   TilePlan t;
   const int variant = g_kernel_variant;
+  if (variant == 0 && plan_lane(*p, &t)) return 0;
   if ((variant == 0 || variant == 3) &&
       plan_tma_tiles(p->nx, p->ny, p->nz, p->num_oris, p->bc_x, d.sm_count, d.smem_per_sm, &t))
     return fixed_plan_index(p->num_oris, t);
@@ -538,7 +583,10 @@ extern "C" int pfg_fixed_plan(const pfg_pf_params* p) {
 extern "C" int pfg_device_error(int clear) {
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
   const int v = read_device_error(clear);
-  return v;
+  const int w = read_lane_device_error(clear);
+  if (v < 0) return v;
+  if (w < 0) return w;
+  return v ? v : w;
 }
 
 extern "C" int pfg_set_kernel_variant(int variant) {
@@ -682,4 +730,43 @@ extern "C" int pfg_heat_pf_step(const pfg_pf_params* p, const pfg_heat_params* h
   a.hc = make_heat_consts(*h);
   a.hp = *h;
   return record_cuda(dispatch<kTHeat>(a, *p, dt, static_cast<cudaStream_t>(stream)));
+}
+
+extern "C" int pfg_heat_pf_step_comp_supported(const pfg_pf_params* p) {
+  int st = check_pf_params(p);
+  if (st) return -st;
+  if (!device_info().ok) return -PFG_ERR_NO_DEVICE;
+  TilePlan t;
+  return (g_kernel_variant == 0 && plan_lane(*p, &t)) ? 1 : 0;
+}
+
+extern "C" int pfg_heat_pf_step_comp(const pfg_pf_params* p, const pfg_heat_params* h,
+                                     const float* eta_in, float* eta_out, const float* Tg_in,
+                                     const float* Tlo_in, float* Tg_out, float* Tlo_out,
+                                     const pfg_clock* clk_in, pfg_clock* clk_out, float dt,
+                                     void* stream) {
+  int st = check_pf_params(p);
+  if (st) return st;
+  st = check_heat_params(h);
+  if (st) return st;
+  if (h->nx != p->nx || h->ny != p->ny || h->nz != p->nz) return PFG_ERR_SHAPE;
+  if (p->bc_x || p->bc_y || p->bc_z) return PFG_ERR_PARAM;  // heat faces are not periodic
+  if (h->layout != PFG_LAYOUT_ZYX) return PFG_ERR_PARAM;
+  if (!eta_in || !eta_out || !Tg_in || !Tg_out || !Tlo_in || !Tlo_out || !clk_in)
+    return PFG_ERR_NULL;
+  if (clk_in == clk_out || Tg_in == Tg_out || Tlo_in == Tlo_out) return PFG_ERR_PARAM;
+  if (!aligned16(eta_in) || !aligned16(eta_out)) return PFG_ERR_ALIGN;
+  if (!device_info().ok) return PFG_ERR_NO_DEVICE;
+  TilePlan t;
+  if (g_kernel_variant != 0 || !plan_lane(*p, &t)) return PFG_ERR_PARAM;
+  StepArgs a{};
+  a.eta_in = eta_in; a.eta_out = eta_out; a.T = Tg_in; a.T_out = Tg_out;
+  a.T_lo = Tlo_in; a.T_lo_out = Tlo_out;
+  a.clk_in = clk_in; a.clk_out = clk_out;
+  a.hc = make_heat_consts(*h);
+  a.hd = make_heat_df(*h, dt);
+  a.hp = *h;
+  fill_common(a, *p, t, dt);
+  a.cpw = t.cpw; a.wx = t.wx; a.rpw = t.rpw;
+  return record_cuda(launch_lane_kernel<kTHeat>(a, t, static_cast<cudaStream_t>(stream)));
 }

@@ -26,6 +26,7 @@
 #include <cmath>
 
 #include "pfg_host.h"
+#include "pfg_mbar.cuh"
 #include "pfg_step.cuh"
 #include "pfg_warp.cuh"
 
@@ -33,52 +34,13 @@ namespace pfg {
 
 __device__ int g_pfg_device_error = 0;  // PFG_ERR_TIMEOUT once a bounded wait ran out
 
-constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at 2 GHz
-
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-  return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count));
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_mbar_arrive_noinc(uint64_t* bar) {
-  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" ::"r"(smem_addr(bar))
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Wait for the phase with this parity to complete; false if the wait ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) {
-      atomicExch(&g_pfg_device_error, PFG_ERR_TIMEOUT);
-      return false;
-    }
-  }
-  return true;
-}
-__device__ __forceinline__ void tma_row(void* dst, const void* src, unsigned bytes,
-                                        uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::
-          "r"(smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
+// Wait for the phase with this parity to complete; false (and the device
+// error flag set) if the wait ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity,
+                                          long long cycles = kWaitCycles) {
+  if (mbar_wait_for(bar, parity, cycles)) return true;
+  atomicExch(&g_pfg_device_error, PFG_ERR_TIMEOUT);
+  return false;
 }
 
 // Folded update of one element (see pfg_warp.cuh for the derivation).  The
@@ -190,10 +152,12 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   __shared__ double s_t0;
   __shared__ long long s_step;
   __shared__ float s_beam[3];
+  __shared__ uint64_t s_never;  // a barrier nothing arrives on (the wait probe)
   if (threadIdx.x == 0) {
     s_abort = 0;
     // expect-tx arrival of warp 0's lane 0 + one cp.async arrival per thread
     for (int s = 0; s < S; ++s) mbar_init(&full[s], 1 + NC);
+    mbar_init(&s_never, 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     double t = 0.0;
     if constexpr (TSRC != kTArray) {
@@ -404,6 +368,9 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
   int issued = 0;
   for (int j = 0; j < S - 1 && j < nplanes; ++j) { stage(j, j); issued = j + 1; }
   bool ok = true;
+  // wait probe: a wait on a barrier that never completes runs out after
+  // probe_wait cycles and takes the timeout path below
+  if (a.probe_wait > 0) ok = mbar_wait(&s_never, 0u, a.probe_wait);
   for (int j = 0; j < 3 && ok; ++j) ok = mbar_wait(&full[j], 0u);  // S >= 4: first phase
   if (ok) cell_coefs(1, 0, zb);
   else s_abort = 1;
@@ -510,11 +477,12 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
     if (s_next == 0) ph_next ^= 1u;
   }
   // drain: copies still in flight must land before the CTA's shared memory is
-  // released (in a normal run every issued plane has been waited for already)
+  // released (in a normal run every issued plane has been waited for
+  // already).  After a timeout every slot still gets its full bound.
   cp_async_wait(0);
   if (threadIdx.x == 0) {
     for (int j = max(0, issued - S); j < issued; ++j)
-      if (!mbar_wait(&full[j % S], (unsigned)((j / S) & 1))) break;
+      mbar_wait(&full[j % S], (unsigned)((j / S) & 1));
   }
 }
 

@@ -6,6 +6,7 @@
 #include <stdint.h>
 
 #include "pf_gb300.h"
+#include "pfg_df.cuh"
 
 namespace pfg {
 
@@ -238,6 +239,22 @@ __device__ __forceinline__ void laser_at(const pfg_heat_params& hp, double t, fl
   }
 }
 
+// laser_at with the beam centre in float64.
+__device__ __forceinline__ void laser_at_d(const pfg_heat_params& hp, double t, double* xl,
+                                           double* yl, float* P) {
+  *xl = 0.0; *yl = 0.0; *P = 0.f;
+  for (int s = 0; s < hp.num_segments && s < PFG_MAX_SEGMENTS; ++s) {
+    const pfg_segment& g = hp.path[s];
+    if (t >= (double)g.t0 && t < (double)g.t1) {
+      const double f = (t - (double)g.t0) / ((double)g.t1 - (double)g.t0);
+      *xl = (double)g.x0 + f * ((double)g.x1 - (double)g.x0);
+      *yl = (double)g.y0 + f * ((double)g.y1 - (double)g.y0);
+      *P = g.power;
+      return;
+    }
+  }
+}
+
 // New ghosts of the domain faces that interior cell (gx, gy, gz) touches,
 // computed from the old ghost (gamma.py:18-43), written to Tg_out and
 // substituted for the matching neighbour value.  rk = 1 / k(Tc).
@@ -305,6 +322,119 @@ __device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc,
 }
 
 // ---------------------------------------------------------------------------
+// Compensated (double-float) heat update.  The temperature is stored as two
+// float32 fields, T = h + l.  A float32 update rounds T to ulp(T) ~ 1e-3 K
+// every step at T ~ 1e4 K, and the rounded coefficients k / (rho cp) and
+// the rounded beam flux make a run drift from the float64 reference by up
+// to ~1e-2 K over thousands of steps; a cell near Ts, Tl (the latent-heat
+// switch) or T_liquidus then takes the other branch of the step function
+// and differs by O(1 K).  The compensated update keeps the state to ~48
+// bits, forms the Laplacian from exact differences, and, wherever the
+// temperature is far from ambient (or on a domain face), evaluates the
+// coefficients, the Robin/radiation flux and the Gaussian beam in DF.
+// ---------------------------------------------------------------------------
+struct HeatDF {
+  DF k1, k0;          // k = k1 clip(T, 300, Tl) + k0        (gamma.py:14)
+  DF c1, c0, latent;  // cp = c1 clip(T, 300, Tl) + c0 [+ L] (gamma.py:12-15)
+  DF beam_coef;       // 2 absorptivity / (pi r^2)
+  DF two_over_r2;     // 2 / r^2
+  DF sb_eps, T0_4;    // sigma eps, T0^4
+  DF rd2[3];          // 1 / d^2 per axis
+  DF dt;              // the step (a float32 value)
+  float hot;          // a warp with a cell or neighbour above this takes the DF path
+};
+
+// Robin + radiation flux h (Tf - T0) + sigma eps (Tf^4 - T0^4) in DF
+// (gamma.py:23-34), Tf the face temperature.
+__device__ __forceinline__ DF heat_robin_df(const HeatConsts& H, const HeatDF& D, DF Tf) {
+  const DF t2 = df_mul(Tf, Tf);
+  const DF rad = df_mul(D.sb_eps, df_sub(df_mul(t2, t2), D.T0_4));
+  return df_add(df_mul_f(df_add_f(Tf, -H.T0), H.h), rad);
+}
+
+// k(T) and cp(T) in DF (gamma.py:12-15)
+__device__ __forceinline__ void heat_k_cp_df(const HeatConsts& H, const HeatDF& D, DF T, DF& k,
+                                             DF& cp) {
+  const DF clip = df_gt(T, H.Tl) ? df_from(H.Tl) : (df_lt(T, 300.f) ? df_from(300.f) : T);
+  k = df_add(df_mul(D.k1, clip), D.k0);
+  cp = df_add(df_mul(D.c1, clip), D.c0);
+  if (df_gt(T, H.Ts) && df_lt(T, H.Tl)) cp = df_add(cp, D.latent);
+}
+
+// New ghosts of the domain faces the cell touches (gamma.py:18-43), in DF,
+// written to (Th_out, Tl_out) and substituted for the neighbour: ghost =
+// T - q dx / k.  n[] = xm, xp, ym, yp, zm, zp.  (xl, yl): beam centre.
+__device__ __forceinline__ void heat_faces_df(const HeatConsts& H, const HeatDF& D, DF Tc, DF k,
+                                              DF* n, int gx, int gy, int gz, DF xl, DF yl,
+                                              float P, float* Th_out, float* Tl_out, int idx,
+                                              int sx, int sy, int sz) {
+  const int face_idx[6] = {idx - sx, idx + sx, idx - sy, idx + sy, idx - sz, idx + sz};
+  const bool on[6] = {gx == 0, gx == H.nx - 1, gy == 0, gy == H.ny - 1, gz == 0, gz == H.nz - 1};
+  const float d[3] = {H.dx, H.dy, H.dz};
+#pragma unroll
+  for (int f = 0; f < 6; ++f) {
+    if (!on[f]) continue;
+    DF Tf = df_add(Tc, n[f]);
+    Tf.h *= 0.5f;
+    Tf.l *= 0.5f;
+    DF q = heat_robin_df(H, D, Tf);
+    if (f == 5) {
+      // top face: minus the Gaussian beam (gamma.py:33-35), positions exact
+      const DF x = df_add_f(two_prod((float)gx, H.dx), H.x_first);
+      const DF y = df_add_f(two_prod((float)gy, H.dy), H.y_first);
+      const DF ddx = df_sub(x, xl), ddy = df_sub(y, yl);
+      const DF r2 = df_add(df_mul(ddx, ddx), df_mul(ddy, ddy));
+      const DF e = df_exp_neg(df_neg(df_mul(r2, D.two_over_r2)));
+      q = df_sub(q, df_mul_f(df_mul(e, D.beam_coef), P));
+    }
+    const DF g = df_sub(Tc, df_div(df_mul_f(q, d[f >> 1]), k));
+    Th_out[face_idx[f]] = g.h;
+    Tl_out[face_idx[f]] = g.l;
+    n[f] = g;
+  }
+}
+
+// The compensated explicit heat update of one interior cell: returns the
+// new temperature.  DFPATH: coefficients in DF (cells far from ambient and
+// face cells, FACES then true); otherwise float32 coefficients on the exact
+// Laplacian, which keeps ambient regions exact and costs little.
+template <bool FACES, bool DFPATH>
+__device__ __forceinline__ DF heat_cell_update_df(const HeatConsts& H, const HeatDF& D, DF Tc,
+                                                  DF* n, int gx, int gy, int gz, DF xl, DF yl,
+                                                  float P, float dt, float* Th_out,
+                                                  float* Tl_out, int idx, int sx, int sy,
+                                                  int sz) {
+  if constexpr (DFPATH) {
+    DF k, cp;
+    heat_k_cp_df(H, D, Tc, k, cp);
+    if constexpr (FACES)
+      heat_faces_df(H, D, Tc, k, n, gx, gy, gz, xl, yl, P, Th_out, Tl_out, idx, sx, sy, sz);
+    DF lap = df_from(0.f);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const DF s2 = df_add(df_sub(n[2 * a], Tc), df_sub(n[2 * a + 1], Tc));
+      lap = df_add(lap, df_mul(s2, D.rd2[a]));
+    }
+    const DF coef = df_div(df_mul(k, D.dt), df_mul_f(cp, H.rho));
+    return df_add(Tc, df_mul(coef, lap));
+  } else {
+    static_assert(!FACES, "face cells take the DF path");
+    const float k = heat_k(H, Tc.h);
+    const float cp = 0.2441f * fminf(fmaxf(Tc.h, 300.f), H.Tl) + 338.39f +
+                     (heat_mushy(H, Tc.h) ? H.latent : 0.f);
+    const float rd[3] = {H.rdx2, H.rdy2, H.rdz2};
+    float lap = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const float s2 = ((n[2 * a].h - Tc.h) + (n[2 * a + 1].h - Tc.h)) +
+                       ((n[2 * a].l - Tc.l) + (n[2 * a + 1].l - Tc.l));
+      lap = fmaf(s2, rd[a], lap);
+    }
+    return df_add_f(Tc, dt * ((k * H.inv_rho) * rcp_approx(cp) * lap));
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Moving point source (Rosenthal), per cell.
 // ---------------------------------------------------------------------------
 struct PointConsts {
@@ -341,6 +471,7 @@ __device__ __forceinline__ float interp_weight(double t_future, double dt_coarse
 }
 
 HeatConsts make_heat_consts(const pfg_heat_params& h);
+HeatDF make_heat_df(const pfg_heat_params& h, float dt);
 PointConsts make_point_consts(const pfg_point_sources& s, const pfg_pf_params& p);
 PFConsts make_pf_consts(const pfg_pf_params& p);
 

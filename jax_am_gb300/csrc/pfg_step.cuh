@@ -26,12 +26,16 @@ struct __align__(16) StepArgs {
   const pfg_clock* clk_in;
   pfg_clock* clk_out;
   HeatConsts hc;
+  HeatDF hd;           // compensated heat update constants (fused, T_lo set)
+  const float* T_lo;   // low parts of the compensated ghosted T (or nullptr)
+  float* T_lo_out;
   pfg_heat_params hp;  // tool path (fused)
   pfg_quench q;        // moving gradient (quench)
   PointConsts ps;      // moving point source
   const float* T2;     // interpolation: T_future (T holds T_past)
   double t_future, dt_coarse;
   float h_z;
+  long long probe_wait;  // > 0: the wait probe (pfg_tune key 8), cycles
   float dirs[3 * PFG_MAX_ORIS * 3];
 };
 
@@ -56,8 +60,17 @@ template <int TSRC>
 cudaError_t launch_tma_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);
 // Which compile-time plan of the TMA-fed kernel (1 or 2) a TMA plan uses, or 0.
 int fixed_plan_index(int n, const TilePlan& t);
-// The device error flag (PFG_ERR_TIMEOUT after a bounded wait ran out), or a
-// negative pfg_status if it cannot be read; clear != 0 resets it.
+// Cell-per-lane TMA kernel (pf_lane.cu), num_oris = 20.
+bool plan_lane_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_per_sm,
+                     int max_smem_per_block, int zchunks_override, TilePlan* out);
+template <int TSRC>
+cudaError_t launch_lane_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);
+// The device error flags (PFG_ERR_TIMEOUT after a bounded wait ran out) of
+// the TMA-fed and the cell-per-lane kernels, or a negative pfg_status if one
+// cannot be read; clear != 0 resets it.
 int read_device_error(int clear);
+int read_lane_device_error(int clear);
+extern int g_tune_zchunks;
+extern long long g_probe_wait;
 
 }  // namespace pfg

@@ -218,11 +218,15 @@ class PFSolver:
     def write_sols(self, pf_sol, T, step):
         """Write T and the argmax orientation map for step ``step //
         write_sol_interval`` (``allen_cahn.py:182-210``): a VTU file
-        ``<data_dir>/vtk/pf/sols/u<k>.vtu`` with cell data ``T`` and
-        ``ori_inds`` (``vtu.write_vtu``; IPF colours are not written), and a
-        NumPy ``.npz`` of T, ori_inds and the liquid mask under
-        ``<data_dir>/numpy/pf/sols`` (what ``grains.process_eta`` reads).
-        Returns the ``.npz`` path."""
+        ``<data_dir>/vtk/pf/sols/u<k>.vtu`` with cell data ``T``, ``ori_inds``
+        and, when the polycrystal carries the IPF colours of its orientations
+        (``unique_oris_rgb``, (3, num_oris, 3): the x, y and z keys, as the
+        reference's ``Field.get_unique_ori_colors`` gives them), ``ipf_x``,
+        ``ipf_y``, ``ipf_z``: each cell's colour gathered by its argmax
+        orientation, black (0) where T > T_liquidus (``allen_cahn.py:186-
+        196``).  Also a NumPy ``.npz`` of T, ori_inds and the liquid mask
+        under ``<data_dir>/numpy/pf/sols`` (what ``grains.process_eta``
+        reads).  Returns the ``.npz`` path."""
         folder = os.path.join(self.pf_args.get("data_dir", "."), "numpy/pf/sols")
         os.makedirs(folder, exist_ok=True)
         k = step // int(self.pf_args.get("write_sol_interval", 1))
@@ -232,10 +236,23 @@ class PFSolver:
         path = os.path.join(folder, f"u{k:03d}.npz")
         np.savez_compressed(path, T=T.cpu().numpy(), ori_inds=argmax.cpu().numpy(),
                             liquid=liquid.cpu().numpy())
+        cell_data = {"T": T}
+        rgb = getattr(self.polycrystal, "unique_oris_rgb", None)
+        if rgb is not None:
+            rgb = torch.as_tensor(np.asarray(rgb), device="cuda")
+            if rgb.shape[:2] != (3, self.n):
+                raise ValueError(f"unique_oris_rgb has shape {tuple(rgb.shape)}, expected "
+                                 f"(3, {self.n}, k)")
+            inds = argmax.long()
+            for axis, name in enumerate(("ipf_x", "ipf_y", "ipf_z")):
+                c = rgb[axis].index_select(0, inds)
+                c[liquid] = 0
+                cell_data[name] = c
+        cell_data["ori_inds"] = argmax
         from .vtu import write_vtu
         p = self.params
         write_vtu(os.path.join(self.pf_args.get("data_dir", "."), f"vtk/pf/sols/u{k:03d}.vtu"),
-                  (p.nx, p.ny, p.nz), (p.h_x, p.h_y, p.h_z), {"T": T, "ori_inds": argmax})
+                  (p.nx, p.ny, p.nz), (p.h_x, p.h_y, p.h_z), cell_data)
         return path
 
     # ---- extensions ---------------------------------------------------------

@@ -8,8 +8,10 @@ module writes the same file format itself: the structured grid as hexahedra
 (VTK cell type 12), points in float32 or float64, connectivity and offsets in
 int32 or int64 as the size needs, cell data arrays as they are given, all as
 raw little-endian binary appended after the XML header (``encoding="raw"``,
-``header_type="UInt64"``), which ParaView and meshio read.  IPF colours need
-orix's colour key (plotting only) and are not written.
+``header_type="UInt64"``), which ParaView and meshio read.  The IPF colour
+arrays are written when the polycrystal supplies its orientations' colours
+(computing them needs orix's colour key, which is plotting only and not
+reproduced here).
 
 ``read_vtu`` reads back what ``write_vtu`` writes (used by the tests).
 """

@@ -33,6 +33,7 @@ class _GraphRun:
         self.cur = 0
         self.clk = torch.zeros((2, 2), dtype=torch.int64, device="cuda")
         self._graph = None
+        self._graph_src = 0
         self.launches = 0
 
     def _launch(self, src):
@@ -55,15 +56,30 @@ class _GraphRun:
                 src ^= 1
         self.launches = counted  # captured launches run at replay, counted there
         self._graph = g
+        self._graph_src = start  # the buffer the graph reads first (and ends in)
         return 1
 
+    def prepare(self):
+        """Capture the replayed graph now, so that a later ``run`` only
+        replays it.  The capture takes one eager step (kernel attributes are
+        set outside the capture); returns the number of steps taken (1, or 0
+        when the graph exists already)."""
+        if self._graph is not None:
+            return 0
+        return self._capture()
+
     def run(self, steps, graph=True):
-        """Advance ``steps`` steps (graph replay when ``graph``)."""
+        """Advance ``steps`` steps (graph replay when ``graph``).  The graph
+        reads the buffer it was captured from, so after an odd number of
+        eager steps one more eager step comes first."""
         done = 0
         if graph and steps >= self.graph_steps:
             if self._graph is None:
                 done += self._capture()
-            while steps - done >= self.graph_steps:
+            if self.cur != self._graph_src and steps - done > self.graph_steps:
+                self.step()
+                done += 1
+            while self.cur == self._graph_src and steps - done >= self.graph_steps:
                 self._graph.replay()
                 self.launches += self.graph_steps
                 done += self.graph_steps
@@ -164,10 +180,18 @@ def raster(tracks, speed, power, x_start, x_end, t_start=0.0):
 
 
 class HeatPFRun(_GraphRun):
-    """Fused explicit heat + phase-field run with a tool-path laser."""
+    """Fused explicit heat + phase-field run with a tool-path laser.
+
+    ``compensated`` (default: wherever the step kernel supports it, i.e.
+    num_oris = 20) keeps the temperature as two float32 fields whose sum is
+    T (``pfg_heat_pf_step_comp``): a 2000-step laser run then tracks a
+    float64 run to ~1e-5 K instead of ~1e-2 K (plus O(1 K) where a cell near
+    the latent-heat or liquidus switch takes the other branch).
+    ``T_ghosted`` is the float32 temperature (the high part);
+    ``T_ghosted_f64`` the full value."""
 
     def __init__(self, solver: PFSolver, gamma_args, path, dt=None, eta0=None, T_init=None,
-                 t0=0.0):
+                 t0=0.0, compensated=None):
         super().__init__()
         self.solver = solver
         p = solver.params
@@ -184,25 +208,65 @@ class HeatPFRun(_GraphRun):
         else:
             Tg = T_init.to("cuda", torch.float32).reshape(shape).contiguous()
         self.Tg = [Tg.clone(), Tg.clone()]  # edge ghosts stay equal in both buffers
+        supported = solver.lib.pfg_heat_pf_step_comp_supported(ctypes.byref(p)) == 1
+        if compensated is None:
+            compensated = supported
+        elif compensated and not supported:
+            raise ValueError("the compensated fused step needs the cell-per-lane kernel "
+                             "(num_oris = 20)")
+        self.compensated = bool(compensated)
+        self.Tl = [torch.zeros_like(Tg), torch.zeros_like(Tg)] if self.compensated else None
         self.set_time(t0)
 
     def _launch(self, src):
         s = self.solver
-        st = s.lib.pfg_heat_pf_step(ctypes.byref(s.params), ctypes.byref(self.heat),
-                                     _lib.ptr(self.eta[src]), _lib.ptr(self.eta[src ^ 1]),
-                                     _lib.ptr(self.Tg[src]), _lib.ptr(self.Tg[src ^ 1]),
-                                     _lib.ptr(self.clk[src]), _lib.ptr(self.clk[src ^ 1]),
-                                     self.dt, _stream())
-        _lib.check(st, "pfg_heat_pf_step")
+        if self.compensated:
+            st = s.lib.pfg_heat_pf_step_comp(
+                ctypes.byref(s.params), ctypes.byref(self.heat), _lib.ptr(self.eta[src]),
+                _lib.ptr(self.eta[src ^ 1]), _lib.ptr(self.Tg[src]), _lib.ptr(self.Tl[src]),
+                _lib.ptr(self.Tg[src ^ 1]), _lib.ptr(self.Tl[src ^ 1]), _lib.ptr(self.clk[src]),
+                _lib.ptr(self.clk[src ^ 1]), self.dt, _stream())
+            _lib.check(st, "pfg_heat_pf_step_comp")
+        else:
+            st = s.lib.pfg_heat_pf_step(ctypes.byref(s.params), ctypes.byref(self.heat),
+                                         _lib.ptr(self.eta[src]), _lib.ptr(self.eta[src ^ 1]),
+                                         _lib.ptr(self.Tg[src]), _lib.ptr(self.Tg[src ^ 1]),
+                                         _lib.ptr(self.clk[src]), _lib.ptr(self.clk[src ^ 1]),
+                                         self.dt, _stream())
+            _lib.check(st, "pfg_heat_pf_step")
         self.launches += 1
 
     @property
     def state(self):
         return self.eta[self.cur]
 
+    def load(self, eta, T_init=None, t0=0.0):
+        """Copy a new state into the resident buffers (asynchronously on the
+        current stream; host tensors should be pinned): eta into the buffer
+        the next step reads, the ghosted T into both T buffers, the clock to
+        ``t0``.  A captured graph keeps its buffers, so it replays the new
+        state."""
+        p = self.solver.params
+        self.eta[self.cur].copy_(eta.reshape(self.eta[self.cur].shape), non_blocking=True)
+        if T_init is not None:
+            shape = (p.nz + 2, p.ny + 2, p.nx + 2)
+            self.Tg[self.cur].copy_(T_init.reshape(shape), non_blocking=True)
+            self.Tg[self.cur ^ 1].copy_(self.Tg[self.cur], non_blocking=True)
+            if self.compensated:
+                self.Tl[0].zero_()
+                self.Tl[1].zero_()
+        self.set_time(t0)
+        return self
+
     @property
     def T_ghosted(self):
         return self.Tg[self.cur]
+
+    @property
+    def T_ghosted_f64(self):
+        """The ghosted temperature in float64 (high + low part when compensated)."""
+        T = self.Tg[self.cur].double()
+        return T + self.Tl[self.cur].double() if self.compensated else T
 
     @property
     def T_cells(self):

@@ -18,16 +18,16 @@ import torch
 
 
 def _shift(e, axis, step, periodic):
-    """Neighbour along ``axis`` of the (Nz, Ny, Nx, n) grid: +1 or -1."""
+    """Neighbour along ``axis`` of the (Nz, Ny, Nx, n) grid: +1 or -1
+    (periodic wrap, or the edge cell repeated: ``allen_cahn.py:61-66``)."""
     if periodic:
         return torch.roll(e, -step, dims=axis)
     n = e.shape[axis]
-    dev = e.device
+    if n == 1:
+        return e
     if step > 0:
-        idx = torch.cat((torch.arange(1, n, device=dev), torch.tensor([n - 1], device=dev)))
-    else:
-        idx = torch.cat((torch.tensor([0], device=dev), torch.arange(n - 1, device=dev)))
-    return torch.index_select(e, axis, idx)
+        return torch.cat((e.narrow(axis, 1, n - 1), e.narrow(axis, n - 1, 1)), dim=axis)
+    return torch.cat((e.narrow(axis, 0, 1), e.narrow(axis, 0, n - 1)), dim=axis)
 
 
 def pf_increment(eta4, T3, a, dirs, bc=(False, False, False)):
@@ -47,10 +47,13 @@ def pf_increment(eta4, T3, a, dirs, bc=(False, False, False)):
     lap = (((xp - eta4) + (xm - eta4)) / hx ** 2 + ((yp - eta4) + (ym - eta4)) / hy ** 2
            + ((zp - eta4) + (zm - eta4)) / hz ** 2)
     if a["anisotropy"] > 0.0:
-        e = torch.stack((xp - xm, yp - ym, zp - zm), dim=-1)  # (..., n, 3)
-        ee = torch.sum(e * e, dim=-1)
-        proj = torch.einsum("kid,zyxid->zyxik", dirs, e)  # (..., n, 3 axes)
-        m = torch.max(proj * proj, dim=-1).values
+        gx, gy, gz = xp - xm, yp - ym, zp - zm  # central differences, (..., n)
+        ee = gx * gx + gy * gy + gz * gz
+        m = None
+        for k in range(3):  # (d_k . e)^2 for the three rotated cube axes
+            d = dirs[k]  # (n, 3)
+            p = gx * d[:, 0] + gy * d[:, 1] + gz * d[:, 2]
+            m = p * p if m is None else torch.maximum(m, p * p)
         safe = torch.where(ee > 0, ee, torch.ones_like(ee))
         c2 = torch.where(ee > 0, torch.clamp(m / safe, max=1.0), torch.ones_like(ee))
         aniso = 1.0 + a["anisotropy"] * (c2 ** 2 + (1.0 - c2) ** 2)
@@ -94,11 +97,33 @@ def heat_step(Tg, xl, yl, P, dt, g, h):
     return out
 
 
-def coupled_step(eta4, Tg, t, dt, a, g, laser, dirs, force_liquid=False, shift=1.0):
+def pf_increment_chunked(eta4, T3, a, dirs, chunk):
+    """``pf_increment`` with Neumann faces, evaluated ``chunk`` z planes at a
+    time (each chunk with its neighbour planes), so that the float64
+    temporaries of a large grid stay a few planes deep.  Equal to
+    ``pf_increment`` of the whole grid: a chunk's edge planes see their true
+    neighbours, and the edge replication at a chunk's halo only affects the
+    halo planes, whose values are dropped."""
+    nz = eta4.shape[0]
+    out = torch.empty_like(eta4)
+    for z0 in range(0, nz, chunk):
+        z1 = min(z0 + chunk, nz)
+        lo, hi = max(z0 - 1, 0), min(z1 + 1, nz)
+        inc = pf_increment(eta4[lo:hi], T3[lo:hi], a, dirs)
+        out[z0:z1] = inc[z0 - lo:z1 - lo]
+    return out
+
+
+def coupled_step(eta4, Tg, t, dt, a, g, laser, dirs, force_liquid=False, shift=1.0, chunk=None):
     """Fused step: phase field at the start-of-step T, heat with the beam at
-    the mid-step time (same convention as ``pf_oracle.coupled_step``)."""
+    the mid-step time (same convention as ``pf_oracle.coupled_step``).
+    ``chunk``: evaluate the phase field ``chunk`` z planes at a time
+    (``pf_increment_chunked``; Neumann faces, as the heat coupling has)."""
     T3 = Tg[1:-1, 1:-1, 1:-1]
-    eta_new = eta4 + dt * pf_increment(eta4, T3, a, dirs)
+    if chunk:
+        eta_new = eta4 + dt * pf_increment_chunked(eta4, T3, a, dirs, chunk)
+    else:
+        eta_new = eta4 + dt * pf_increment(eta4, T3, a, dirs)
     if force_liquid:
         eta_new = torch.where((T3 > a["T_liquidus"] + shift)[..., None],
                               torch.zeros_like(eta_new), eta_new)

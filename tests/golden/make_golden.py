@@ -1,5 +1,5 @@
 """Generate the golden vectors in ``tests/golden/*.npz`` by running the
-reference's OWN source files (JAX-AM, read from /root/reference) in this
+reference's OWN source files (JAX-AM, from the tree given by --ref or JAX_AM_REF) in this
 container.
 
 JAX is not installed and cannot be, so ``jax_standin.py`` supplies ``jax`` /
@@ -18,7 +18,8 @@ What is exercised, unmodified:
 * ``applications/phase_field/{solidification,simple,multi_scan}/example.py``:
   ``get_T_fn`` and ``read_path``.
 
-Run from the repository root:  ``python tests/golden/make_golden.py``
+Run from the repository root:
+``python tests/golden/make_golden.py --ref <reference tree>``
 """
 import contextlib
 import importlib.util
@@ -33,8 +34,10 @@ from unittest import mock
 import numpy as onp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
 sys.path.insert(0, HERE)
+from ref_path import reference_root  # noqa: E402
+
+REF = reference_root()
 import jax_standin  # noqa: E402
 
 jax_standin.install()

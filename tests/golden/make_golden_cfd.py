@@ -1,5 +1,5 @@
 """Generate ``tests/golden/cfd_am3d.npz`` by running the reference's OWN
-``jax_am/cfd/cfd_am.py`` (read from /root/reference) in this container.
+``jax_am/cfd/cfd_am.py`` (from the tree given by --ref or JAX_AM_REF) in this container.
 
 JAX is not installed and cannot be, so ``jax_standin.py`` supplies ``jax``
 (NumPy arithmetic, PyTorch autograd for ``jax.jacrev``, a restatement of
@@ -14,7 +14,8 @@ condition), ``update_convective_terms`` (``get_face_vels``, ``div``),
 ``gradient``, the tool path and the moving local box, for a surface-flux case
 and a body-source case.
 
-Run from the repository root:  ``python tests/golden/make_golden_cfd.py``
+Run from the repository root:
+``python tests/golden/make_golden_cfd.py --ref <reference tree>``
 """
 import contextlib
 import importlib.util
@@ -26,8 +27,10 @@ import tempfile
 import numpy as onp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
 sys.path.insert(0, HERE)
+from ref_path import reference_root  # noqa: E402
+
+REF = reference_root()
 import jax_standin  # noqa: E402
 
 jax_standin.install()

@@ -15,7 +15,8 @@ Cases: Voronoi-like orientation maps with a liquid pool (T above the
 liquidus), isolated single cells, 2- to 4-cell grains (aspect ratio 1 by the
 reference's small-grain rule), straight rods and thin plates.
 
-Run from the repository root:  ``python tests/golden/make_golden_grains.py``
+Run from the repository root:
+``python tests/golden/make_golden_grains.py --ref <reference tree>``
 """
 import contextlib
 import importlib.util
@@ -28,8 +29,10 @@ from unittest import mock
 import numpy as onp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
 sys.path.insert(0, HERE)
+from ref_path import reference_root  # noqa: E402
+
+REF = reference_root()
 import jax_standin  # noqa: E402
 
 jax_standin.install()

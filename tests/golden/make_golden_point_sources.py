@@ -9,7 +9,8 @@ by running their unmodified ``get_T_fn`` (and ``read_path``) under the
 * ``applications/phase_field/multi_scan/example.py:33-84`` at several steps
   of its sampled raster path.
 
-Run from the repository root:  ``python tests/golden/make_golden_point_sources.py``
+Run from the repository root:
+``python tests/golden/make_golden_point_sources.py --ref <reference tree>``
 """
 import contextlib
 import io

@@ -28,7 +28,7 @@ def test_convert_temperature_is_the_transpose(shape):
     np.testing.assert_array_equal(got, np.transpose(T, (2, 1, 0)).reshape(-1, 1))
 
 
-@pytest.fixture(params=[0, 1, 2], ids=["auto", "generic", "warp_cpasync"])
+@pytest.fixture(params=[0, 1, 2, 3], ids=["auto", "generic", "warp_cpasync", "tma256"])
 def variant(request):
     from jax_am_gb300 import _lib
     lib = _lib.load()

@@ -152,12 +152,13 @@ def _laser_fn(path):
     return laser
 
 
-@pytest.fixture(params=[0, 1, 2, 512], ids=["auto", "generic", "warp_cpasync", "tma512"])
+@pytest.fixture(params=[0, 1, 2, 3, 512],
+                ids=["auto", "generic", "warp_cpasync", "tma256", "tma512"])
 def variant(request):
     from jax_am_gb300 import _lib
     lib = _lib.load()
     if request.param == 512:  # the TMA-fed kernel with one 512-thread CTA per SM
-        assert lib.pfg_set_kernel_variant(0) == 0 and lib.pfg_tune(5, 512) == 0
+        assert lib.pfg_set_kernel_variant(3) == 0 and lib.pfg_tune(5, 512) == 0
     else:
         assert lib.pfg_set_kernel_variant(request.param) == 0
     yield request.param
@@ -192,7 +193,7 @@ def test_fused_heat_pf_vs_oracle(shape, n, aniso, steps, variant):
         e_ref, T_ref = O.coupled_step(e_ref, T_ref, t, dt, oargs, g, laser,
                                       poly.unique_grain_directions)
         t += dt
-    T_gpu = run.T_ghosted.double().cpu().numpy().transpose(2, 1, 0)
+    T_gpu = run.T_ghosted_f64.cpu().numpy().transpose(2, 1, 0)
     e_gpu = run.state.double().cpu().numpy()
     I = (slice(1, -1),) * 3
     t_err = np.abs(T_gpu[I] - T_ref[I]).max()

@@ -25,13 +25,14 @@ def _built():
     _build.build()
 
 
-@pytest.fixture(params=[0, 1, 2, 512], ids=["auto", "generic", "warp_cpasync", "tma512"])
+@pytest.fixture(params=[0, 1, 2, 3, 512],
+                ids=["auto", "generic", "warp_cpasync", "tma256", "tma512"])
 def variant(request):
     """Run a test on the warp-per-cells kernel and on the generic kernel."""
     from jax_am_gb300 import _lib
     lib = _lib.load()
     if request.param == 512:  # the TMA-fed kernel with one 512-thread CTA per SM
-        assert lib.pfg_set_kernel_variant(0) == 0 and lib.pfg_tune(5, 512) == 0
+        assert lib.pfg_set_kernel_variant(3) == 0 and lib.pfg_tune(5, 512) == 0
     else:
         assert lib.pfg_set_kernel_variant(request.param) == 0
     yield request.param
@@ -237,13 +238,13 @@ def test_warp_and_generic_kernels_agree(n, aniso):
     lib = _lib.load()
     poly, eta, T, pf_args, oargs, obc = pf_case((41, 29, 13), n, aniso, seed=n)
     outs = []
-    for v in (0, 1, 2):
+    for v in (0, 1, 2, 3):
         lib.pfg_set_kernel_variant(v)
         s = _solver(pf_args, poly)
         outs.append(_run_gpu(s, eta, T, 1e-8, 4))
     lib.pfg_set_kernel_variant(0)
-    assert np.abs(outs[0] - outs[1]).max() <= 1e-5
-    assert np.abs(outs[2] - outs[1]).max() <= 1e-5
+    for o in (outs[0], outs[2], outs[3]):
+        assert np.abs(o - outs[1]).max() <= 1e-5
     assert _lib.device_error() == 0
 
 
@@ -251,7 +252,9 @@ def test_plans_report_the_kernel_used():
     from jax_am_gb300 import _lib
     from jax_am_gb300.phase_field.allen_cahn import make_pf_params
     lib = _lib.load()
-    for shape, n, bc, kernel, vec in (((30, 20, 10), 20, None, 3, 4), ((30, 20, 10), 12, None, 3, 4),
+    for shape, n, bc, kernel, vec in (((30, 20, 10), 20, None, 4, 4),
+                                      ((30, 20, 10), 20, "periodic", 4, 4),
+                                      ((30, 20, 10), 12, None, 3, 4),
                                       ((30, 20, 10), 10, None, 3, 2), ((30, 20, 10), 30, None, 3, 2),
                                       ((31, 20, 10), 30, None, 2, 2),
                                       ((30, 20, 10), 30, "periodic", 2, 2),
@@ -261,6 +264,9 @@ def test_plans_report_the_kernel_used():
         assert plan["kernel"] == kernel and plan["vec"] == vec, (shape, n, bc, plan)
     lib.pfg_set_kernel_variant(1)
     assert _lib.describe_plan(make_pf_params(pf_args, poly))["kernel"] == 1
+    poly, eta, T, pf_args, _, _ = pf_case((30, 20, 10), 20, 0.15, seed=20)
+    lib.pfg_set_kernel_variant(3)  # the TMA-fed kernel ahead of the cell-per-lane kernel
+    assert _lib.describe_plan(make_pf_params(pf_args, poly))["kernel"] == 3
     lib.pfg_set_kernel_variant(0)
 
 
@@ -283,3 +289,35 @@ def test_rk4_vs_oracle(aniso):
     print(f"rk4 A={aniso}: max |d eta| = {err:.3e}")
     assert err <= ETA_TOL
     assert _argmax_mismatch(got, ref) == 0
+
+
+def test_liquidus_not_a_float32_value():
+    """T_liquidus = 1623.1 K has no float32 value.  The C ABI holds it as a
+    float32 (``pfg_pf_params.T_liquidus``), so the step compares T with
+    float32(1623.1) exactly as the reference does on float32 arrays (NumPy
+    and jax.numpy round the Python float to the array's float32): a cell at
+    T = float32(1623.1) has T / T_liquidus = 1 and zeta = 1/2.  Checked
+    against the oracle given the float32-rounded T_liquidus, on cells placed
+    exactly there and one float32 step either side, and the inspect metrics
+    count T >= float32(1623.1) as liquid."""
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    poly, eta, T, pf_args, oargs, obc = pf_case((12, 9, 7), 20, 0.15, seed=31)
+    tl32 = np.float32(1623.1)
+    T = T.copy()
+    T[0::5] = float(tl32)
+    T[1::5] = float(np.nextafter(tl32, np.float32(np.inf)))
+    T[2::5] = float(np.nextafter(tl32, np.float32(-np.inf)))
+    pf_args = dict(pf_args, T_liquidus=1623.1)
+    oargs = dict(oargs, T_liquidus=float(tl32))
+    s = PFSolver(pf_args, poly)
+    got = _run_gpu(s, eta, T, 1e-8, 3)
+    ref = _run_oracle(eta, T, oargs, poly.unique_grain_directions, obc, 1e-8, 3)
+    err = np.abs(got - ref).max()
+    print(f"T_liquidus 1623.1 (float32 {float(tl32)!r}): max |d eta| = {err:.3e}")
+    assert err <= ETA_TOL
+    assert _argmax_mismatch(got, ref) == 0
+    d = s.inspect_sol(torch.tensor(eta, dtype=torch.float32, device="cuda"),
+                      torch.tensor(eta, dtype=torch.float32, device="cuda"),
+                      torch.tensor(T, dtype=torch.float32, device="cuda"), [0.0, 1e-8], 1)
+    want = 100.0 * np.mean(T.astype(np.float32).reshape(-1) >= tl32)
+    assert abs(d["pct_liquid"] - want) <= 1e-9

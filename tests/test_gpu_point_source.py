@@ -63,7 +63,7 @@ def test_T_matches_reference_drivers(kind):
     print(f"{kind}: max relative |dT| vs reference = {worst:.2e}")
 
 
-@pytest.fixture(params=[0, 1, 2], ids=["auto", "generic", "warp_cpasync"])
+@pytest.fixture(params=[0, 1, 2, 3], ids=["auto", "generic", "warp_cpasync", "tma256"])
 def variant(request):
     from jax_am_gb300 import _lib
     lib = _lib.load()

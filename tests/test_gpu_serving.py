@@ -110,3 +110,16 @@ def test_realtime_arrivals_are_admitted_while_others_run():
     for j in jobs:
         assert j.finished >= j.arrival and j.admitted >= j.arrival
     print(out)
+
+
+def test_resident_sequential_baseline_matches_stepper():
+    """The graph-replayed per-job baseline (QuenchRun) gives the per-step
+    stepper's results (the same kernels, launched from a graph)."""
+    from jax_am_gb300.serving import run_sequential, run_sequential_resident
+    a, b = _mix(), _mix()
+    ra = run_sequential(a, realtime=False)
+    rb = run_sequential_resident(b, realtime=False)
+    assert ra["jobs"] == rb["jobs"] == len(a)
+    for ja, jb in zip(a, b):
+        assert torch.equal(ja.result, jb.result), (ja.cells, ja.num_oris, ja.steps)
+
