@@ -192,7 +192,19 @@ __global__ void __launch_bounds__(256, 2) pf_lane_kernel(const __grid_constant__
   const unsigned plane_bytes =
       (unsigned)rows * (row_bytes + (wrap_left ? cell_bytes : 0u) + (wrap_right ? cell_bytes : 0u));
   const int gsy = a.nx + 2, gsz = (a.ny + 2) * (a.nx + 2);  // ghosted strides (host checks < 2^31)
-  const int tcols = txv + 2;
+  // this thread's ghosted temperature cells of a staged plane (at most two):
+  // offsets from the tile's first ghosted cell and in the slot, or -1
+  int t_src[2], t_dst[2];
+  if constexpr (HEAT) {
+    const int tcols = txv + 2;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int i = threadIdx.x + q * NC;
+      const int r = i / tcols, c = i - r * tcols;
+      t_src[q] = r < rows ? r * gsy + c : -1;
+      t_dst[q] = r * TPX + c;
+    }
+  }
   auto stage = [&](int j) {
     const int s = j % S;
     const int pz = zb - 1 + j;
@@ -211,17 +223,14 @@ __global__ void __launch_bounds__(256, 2) pf_lane_kernel(const __grid_constant__
       }
     }
     if constexpr (HEAT) {
-      // this thread's ghosted temperature cells of the plane (at most two)
       float* ts = T_s + s * TSLOT;
       const float* tplane = a.T + (int64_t)(pz + 1) * gsz + (int64_t)y0 * gsy + x0;
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
-        const int i = threadIdx.x + q * NC;
-        const int r = i / tcols, c = i - r * tcols;
-        if (r < rows) {
-          cp_async<4>(ts + r * TPX + c, tplane + r * gsy + c);
+        if (t_src[q] >= 0) {
+          cp_async<4>(ts + t_dst[q], tplane + t_src[q]);
           if constexpr (COMP)
-            cp_async<4>(TL_s + s * TSLOT + r * TPX + c, a.T_lo + (tplane - a.T) + r * gsy + c);
+            cp_async<4>(TL_s + s * TSLOT + t_dst[q], a.T_lo + (tplane - a.T) + t_src[q]);
         }
       }
       cp_async_mbar_arrive_noinc(&full[s]);
@@ -333,16 +342,19 @@ __global__ void __launch_bounds__(256, 2) pf_lane_kernel(const __grid_constant__
           const float tmax = fmaxf(fmaxf(fmaxf(Tc, Txm), fmaxf(Txp, Tym)),
                                    fmaxf(fmaxf(Typ, Tzm), Tzp));
           DF Tn = c;
-          if (__any_sync(0xffffffffu, on_face && valid)) {
+          // warp-uniform choice: DF arithmetic where the temperature is far
+          // from ambient or the beam heats the top face
+          if (__any_sync(0xffffffffu, valid && (tmax > a.hd.hot || z == a.nz - 1))) {
             if (valid)
-              Tn = heat_cell_update_df<true, true>(a.hc, a.hd, c, n, gx, gy, z, xld, yld, Pw,
-                                                   a.dt, a.T_out, a.T_lo_out, idx, 1, gsy, gsz);
-          } else if (__any_sync(0xffffffffu, valid && tmax > a.hd.hot)) {
-            Tn = heat_cell_update_df<false, true>(a.hc, a.hd, c, n, gx, gy, z, xld, yld, Pw, a.dt,
-                                                  a.T_out, a.T_lo_out, idx, 1, gsy, gsz);
+              Tn = heat_update_df_accurate(a.hc, a.hd, c, n, gx, gy, z, xld, yld, Pw, a.T_out,
+                                           a.T_lo_out, idx, 1, gsy, gsz);
+          } else if (__any_sync(0xffffffffu, on_face && valid)) {
+            if (valid)
+              Tn = heat_update_df_near_ambient<true>(a.hc, c, n, gx, gy, z, xl, yl, Pw, a.dt,
+                                                     a.T_out, a.T_lo_out, idx, 1, gsy, gsz);
           } else {
-            Tn = heat_cell_update_df<false, false>(a.hc, a.hd, c, n, gx, gy, z, xld, yld, Pw,
-                                                   a.dt, a.T_out, a.T_lo_out, idx, 1, gsy, gsz);
+            Tn = heat_update_df_near_ambient<false>(a.hc, c, n, gx, gy, z, xl, yl, Pw, a.dt,
+                                                    a.T_out, a.T_lo_out, idx, 1, gsy, gsz);
           }
           if (valid) {
             a.T_out[idx] = Tn.h;
@@ -382,7 +394,10 @@ __global__ void __launch_bounds__(256, 2) pf_lane_kernel(const __grid_constant__
         s_a = fmaf(u.x, u.x, fmaf(u.y, u.y, s_a));
         s_b = fmaf(u.z, u.z, fmaf(u.w, u.w, s_b));
       }
-      const float4 k = lane_fold(a.pc, temp_coefficients_fast(a.pc, Tcell, a.dt), s_a + s_b);
+      TempCoef tcf;
+      if constexpr (COMP) tcf = temp_coefficients_pair(a.pc, Tcell, Lc, a.dt);
+      else tcf = temp_coefficients_fast(a.pc, Tcell, a.dt);
+      const float4 k = lane_fold(a.pc, tcf, s_a + s_b);
       // ---- element updates, one 16-byte vector of orientations at a time
       const float* p1 = e1 + own;
       const float* p2 = e2 + own;

@@ -160,6 +160,22 @@ __device__ __forceinline__ TempCoef temp_coefficients_fast(const PFConsts& c, fl
   return r;
 }
 
+// temp_coefficients_fast for a compensated temperature Th + Tl: zeta from
+// the exact sign of Th + Tl - T_liquidus (the float64 reference's tanh of
+// 1e10 (T / T_liq - 1) is +-1 unless |T - T_liq| < ~1e-6 K), Lg from Th.
+__device__ __forceinline__ TempCoef temp_coefficients_pair(const PFConsts& c, float Th, float Tl,
+                                                           float dt) {
+  TempCoef r = temp_coefficients_fast(c, Th, dt);
+  if (Th <= 2000.f && Th == c.T_liq && Tl != 0.f) {
+    const float om = (Tl > 0.f) ? 1.f : 0.f;  // 1 - zeta
+    r.om2 = 2.f * om * om;
+  } else if (Th <= 2000.f && Th > c.zeta_lo && Th < c.zeta_hi && Th != c.T_liq) {
+    const float om = (Th > c.T_liq) ? 1.f : 0.f;
+    r.om2 = 2.f * om * om;
+  }
+  return r;
+}
+
 __device__ __forceinline__ CellCoef cell_coefficients(const TempCoef& t, float S) {
   CellCoef r;
   r.cg = t.cg;
@@ -394,44 +410,73 @@ __device__ __forceinline__ void heat_faces_df(const HeatConsts& H, const HeatDF&
   }
 }
 
-// The compensated explicit heat update of one interior cell: returns the
-// new temperature.  DFPATH: coefficients in DF (cells far from ambient and
-// face cells, FACES then true); otherwise float32 coefficients on the exact
-// Laplacian, which keeps ambient regions exact and costs little.
-template <bool FACES, bool DFPATH>
-__device__ __forceinline__ DF heat_cell_update_df(const HeatConsts& H, const HeatDF& D, DF Tc,
-                                                  DF* n, int gx, int gy, int gz, DF xl, DF yl,
-                                                  float P, float dt, float* Th_out,
-                                                  float* Tl_out, int idx, int sx, int sy,
-                                                  int sz) {
-  if constexpr (DFPATH) {
-    DF k, cp;
-    heat_k_cp_df(H, D, Tc, k, cp);
-    if constexpr (FACES)
-      heat_faces_df(H, D, Tc, k, n, gx, gy, gz, xl, yl, P, Th_out, Tl_out, idx, sx, sy, sz);
-    DF lap = df_from(0.f);
+// The compensated explicit heat update of one interior cell, all in DF:
+// k and cp, the new ghosts of the faces the cell touches (Robin/radiation
+// and the Gaussian beam), the Laplacian and the update.  For cells far from
+// ambient and the beam-heated top plane; kept out of line so that the
+// stencil loop stays small.
+static __device__ __noinline__ DF heat_update_df_accurate(const HeatConsts& H, const HeatDF& D,
+                                                          DF Tc, DF* n, int gx, int gy, int gz,
+                                                          DF xl, DF yl, float P, float* Th_out,
+                                                          float* Tl_out, int idx, int sx, int sy,
+                                                          int sz) {
+  DF k, cp;
+  heat_k_cp_df(H, D, Tc, k, cp);
+  heat_faces_df(H, D, Tc, k, n, gx, gy, gz, xl, yl, P, Th_out, Tl_out, idx, sx, sy, sz);
+  DF lap = df_from(0.f);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const DF s2 = df_add(df_sub(n[2 * a], Tc), df_sub(n[2 * a + 1], Tc));
-      lap = df_add(lap, df_mul(s2, D.rd2[a]));
-    }
-    const DF coef = df_div(df_mul(k, D.dt), df_mul_f(cp, H.rho));
-    return df_add(Tc, df_mul(coef, lap));
-  } else {
-    static_assert(!FACES, "face cells take the DF path");
-    const float k = heat_k(H, Tc.h);
-    const float cp = 0.2441f * fminf(fmaxf(Tc.h, 300.f), H.Tl) + 338.39f +
-                     (heat_mushy(H, Tc.h) ? H.latent : 0.f);
-    const float rd[3] = {H.rdx2, H.rdy2, H.rdz2};
-    float lap = 0.f;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float s2 = ((n[2 * a].h - Tc.h) + (n[2 * a + 1].h - Tc.h)) +
-                       ((n[2 * a].l - Tc.l) + (n[2 * a + 1].l - Tc.l));
-      lap = fmaf(s2, rd[a], lap);
-    }
-    return df_add_f(Tc, dt * ((k * H.inv_rho) * rcp_approx(cp) * lap));
+  for (int a = 0; a < 3; ++a) {
+    const DF s2 = df_add(df_sub(n[2 * a], Tc), df_sub(n[2 * a + 1], Tc));
+    lap = df_add(lap, df_mul(s2, D.rd2[a]));
   }
+  const DF coef = df_div(df_mul(k, D.dt), df_mul_f(cp, H.rho));
+  return df_add(Tc, df_mul(coef, lap));
+}
+
+// The compensated update of a cell near ambient: float32 coefficients and
+// face fluxes (their rounding, ~1e-7 of the increment, is far below 1e-6 K
+// when T - T0 < 50 K), the Laplacian from exact differences of the pairs,
+// and the state and the new ghosts kept as pairs.  FACES: the cell may
+// touch a domain face.
+template <bool FACES>
+__device__ __forceinline__ DF heat_update_df_near_ambient(const HeatConsts& H, DF Tc, DF* n,
+                                                         int gx, int gy, int gz, float xl,
+                                                         float yl, float P, float dt,
+                                                         float* Th_out, float* Tl_out, int idx,
+                                                         int sx, int sy, int sz) {
+  const float k = heat_k(H, Tc.h);
+  const float cp = 0.2441f * fminf(fmaxf(Tc.h, 300.f), H.Tl) + 338.39f +
+                   (heat_mushy(H, Tc.h) ? H.latent : 0.f);
+  if constexpr (FACES) {
+    const float rk = rcp_approx(k);
+    const int fidx[6] = {idx - sx, idx + sx, idx - sy, idx + sy, idx - sz, idx + sz};
+    const bool on[6] = {gx == 0, gx == H.nx - 1, gy == 0, gy == H.ny - 1, gz == 0, gz == H.nz - 1};
+    const float d[3] = {H.dx, H.dy, H.dz};
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      if (!on[f]) continue;
+      float q = heat_robin(H, (Tc.h + n[f].h) * 0.5f);
+      if (f == 5) {
+        const float x = H.x_first + (float)gx * H.dx;
+        const float y = H.y_first + (float)gy * H.dy;
+        const float ddx = x - xl, ddy = y - yl;
+        q -= P * H.beam_coef * expf(-(ddx * ddx + ddy * ddy) * H.two_over_r2);
+      }
+      const DF g = df_add_f(Tc, -q * rk * d[f >> 1]);
+      Th_out[fidx[f]] = g.h;
+      Tl_out[fidx[f]] = g.l;
+      n[f] = g;
+    }
+  }
+  const float rd[3] = {H.rdx2, H.rdy2, H.rdz2};
+  float lap = 0.f;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float s2 = ((n[2 * a].h - Tc.h) + (n[2 * a + 1].h - Tc.h)) +
+                     ((n[2 * a].l - Tc.l) + (n[2 * a + 1].l - Tc.l));
+    lap = fmaf(s2, rd[a], lap);
+  }
+  return df_add_f(Tc, dt * ((k * H.inv_rho) * rcp_approx(cp) * lap));
 }
 
 // ---------------------------------------------------------------------------
