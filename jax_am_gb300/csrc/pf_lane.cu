@@ -398,6 +398,9 @@ __global__ void __launch_bounds__(256, 2) pf_lane_kernel(const __grid_constant__
       if constexpr (COMP) tcf = temp_coefficients_pair(a.pc, Tcell, Lc, a.dt);
       else tcf = temp_coefficients_fast(a.pc, Tcell, a.dt);
       const float4 k = lane_fold(a.pc, tcf, s_a + s_b);
+      // the skip below needs finite coefficients in every cell of the warp
+      const bool kfinite = __all_sync(0xffffffffu, !valid || (isfinite(k.x) && isfinite(k.y) &&
+                                                               isfinite(k.z) && isfinite(k.w)));
       // ---- element updates, one 16-byte vector of orientations at a time
       const float* p1 = e1 + own;
       const float* p2 = e2 + own;
@@ -406,7 +409,22 @@ __global__ void __launch_bounds__(256, 2) pf_lane_kernel(const __grid_constant__
         const float4 xm = lds4(p1 + oxm + 4 * v), xp = lds4(p1 + oxp + 4 * v);
         const float4 ym = lds4(p1 - ROWF + 4 * v), yp = lds4(p1 + ROWF + 4 * v);
         const float4 zp = lds4(p2 + 4 * v);
-        float r[4];
+        // Exact zeros: a vector of orientations that is zero (+0.0) at every
+        // cell of the warp and at all their six neighbours stays exactly
+        // zero (gradient, Laplacian and local term vanish, and the update of
+        // +0.0 is +0.0 with finite coefficients), so the warp skips its
+        // arithmetic.  Grain interiors and the far side of an interface are
+        // such zeros.
+        unsigned bits = 0u;
+        {
+          const float4 w[7] = {cc[v], zm[v], xm, xp, ym, yp, zp};
+#pragma unroll
+          for (int i = 0; i < 7; ++i)
+            bits |= __float_as_uint(w[i].x) | __float_as_uint(w[i].y) |
+                    __float_as_uint(w[i].z) | __float_as_uint(w[i].w);
+        }
+        float r[4] = {0.f, 0.f, 0.f, 0.f};
+        if (!kfinite || __any_sync(0xffffffffu, bits != 0u))
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int o = 4 * v + q;  // orientation
