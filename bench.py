@@ -35,8 +35,9 @@ PF_KEYS = dict(T_liquidus=1623.0, gas_const=8.3, Qg=1.4e5, L0=3.5e3, kappa_g=2.7
                ad_hoc=1.0)
 METRIC = "cell_orientation_updates_per_s"
 UNIT = "cell*ori/s"
-KERNEL = ("pf_lane_kernel<NV=5, ANISO=true, TSRC=heat, TX=16, S=4> (fused heat + anisotropic "
-          "phase field, one cell per thread, 16x16 tiles, 4-slot TMA ring)")
+KERNEL = ("pf_lane_kernel<NV=5, ANISO=true, TSRC=heat, TX=16, S=4, COMP=true> (fused "
+          "compensated heat + anisotropic phase field, one cell per thread, 16x16 tiles, "
+          "4-slot TMA ring)")
 
 
 def gamma_args(w):
@@ -136,7 +137,7 @@ def measured_peak():
 
 def traffic_per_launch():
     """DRAM bytes per launch of the top kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "pf_tma_laser_track_8M.md")
+    path = os.path.join(ROOT, "profiles", "pf_lane_laser_track_8M.md")
     if not os.path.exists(path):
         return None
     for line in open(path):
