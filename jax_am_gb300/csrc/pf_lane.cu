@@ -1,8 +1,8 @@
 // Cell-per-lane TMA stencil step: the fast path for num_oris = 20 (every
 // configuration of the reference), with 16-byte orientation vectors.
 //
-// Each thread owns one cell of a TX x TY tile (TX * TY = 256: one cell per
-// thread) and marches it through a chunk of z planes.  All per-cell work is
+// Each thread owns one cell of a TX x TY tile (TX * TY = the CTA's threads:
+// one cell per thread) and marches it through a chunk of z planes.  All per-cell work is
 // done by the thread that owns the cell, in registers: the sum S of eta^2,
 // zeta and the Arrhenius factor, the folded coefficients and the fused heat
 // update.  Nothing per cell goes through shared memory, there are no
@@ -101,18 +101,19 @@ __device__ __forceinline__ float comp(const float4& v, int q) {
   return q == 0 ? v.x : (q == 1 ? v.y : (q == 2 ? v.z : v.w));
 }
 
-// NV: 16-byte vectors per cell (num_oris = 4 NV); TX: tile width (16 or 32;
-// the tile is TX x 256/TX cells); S: ring slots (3 or 4); COMP: the fused
-// heat state is compensated (T = T + T_lo, double-float update).
+// NV: 16-byte vectors per cell (num_oris = 4 NV); NC threads, MINB CTAs per
+// SM; TX: tile width (16 or 32; the tile is TX x NC/TX cells); S: ring slots
+// (3 or 4); COMP: the fused heat state is compensated (T = T + T_lo,
+// double-float update).
 //
 // Ring: plane j (grid plane zb - 1 + j) sits in slot j % S and its copies
 // complete phase (j / S) & 1 of that slot's barrier.  Iteration m (z =
 // zb + m) reads plane m + 1 (the x/y neighbours) and plane m + 2 (the cell
 // above); plane m was last read in iteration m - 1, so right after the
 // barrier that opens iteration m its slot takes plane m + S.
-template <int NV, bool ANISO, int TSRC, int TX, int S, bool COMP>
-__global__ void __launch_bounds__(256, 2) pf_lane_kernel(const __grid_constant__ StepArgs a) {
-  constexpr int NC = 256;
+template <int NV, bool ANISO, int TSRC, int NC, int MINB, int TX, int S, bool COMP>
+__global__ void __launch_bounds__(NC, MINB) pf_lane_kernel(const __grid_constant__ StepArgs a) {
+  static_assert(NC % TX == 0 && NC % 32 == 0, "whole rows, whole warps");
   constexpr int TY = NC / TX;
   constexpr int N = 4 * NV;
   constexpr int TPX = TX + 2, TPY = TY + 2;  // staged tile with its halo
@@ -459,13 +460,15 @@ __global__ void __launch_bounds__(256, 2) pf_lane_kernel(const __grid_constant__
 // ---------------------------------------------------------------------------
 
 constexpr int kLaneNV = 5;   // num_oris = 20
-constexpr int kLaneTX = 16;  // 16 x 16 tiles
+constexpr int kLaneNC = 256;  // threads per CTA: one cell each
+constexpr int kLaneCTAs = 2;  // CTAs per SM
+constexpr int kLaneTX = 16;   // 16 x 16 tiles
 constexpr int kLaneS = 4;    // ring slots
 
 // Shared memory of one CTA: the eta ring, the temperature ring (high and
 // low parts), the barriers.
 static size_t lane_smem(int n, int tx, int slots) {
-  const int ty = 256 / tx;
+  const int ty = kLaneNC / tx;
   const size_t slot = (size_t)(ty + 2) * (tx + 2) * n * 4;
   const size_t tslot = (size_t)(((tx + 2) * (ty + 2) + 3) / 4 * 4) * 4;
   return (size_t)slots * (slot + 2 * tslot) + (size_t)slots * sizeof(uint64_t);
@@ -476,11 +479,12 @@ bool plan_lane_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
   if (n != 4 * kLaneNV) return false;
   // ghosted temperature offsets are 32-bit in this kernel
   if ((int64_t)(nx + 2) * (ny + 2) * (nz + 2) >= ((int64_t)1 << 31)) return false;
-  const int tx = kLaneTX, ty = 256 / tx, S = kLaneS;
+  const int tx = kLaneTX, ty = kLaneNC / tx, S = kLaneS;
   const size_t smem = lane_smem(n, tx, S);
-  // two CTAs per SM: the dynamic shared memory plus the static variables and
+  // kLaneCTAs CTAs per SM: the dynamic shared memory plus the static variables and
   // the per-CTA reservation
-  if (2 * (smem + 1024 + 128) > (size_t)max_smem_per_sm || smem > (size_t)max_smem_per_block)
+  if (kLaneCTAs * (smem + 1024 + 128) > (size_t)max_smem_per_sm ||
+      smem > (size_t)max_smem_per_block)
     return false;
   TilePlan t{};
   t.vec = 4;
@@ -490,14 +494,14 @@ bool plan_lane_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
   t.cpw = 32;
   t.wx = 1;
   t.rpw = 32 / tx;
-  t.rs = 256;
+  t.rs = kLaneNC;
   t.stages = S;
   t.pitch = (tx + 2) * n;
   t.tslot = ((tx + 2) * (ty + 2) + 3) / 4 * 4;
   t.tiles_x = (nx + tx - 1) / tx;
   t.tiles_y = (ny + ty - 1) / ty;
   const long tiles = (long)t.tiles_x * t.tiles_y;
-  const long slots_gpu = 2L * sm_count;
+  const long slots_gpu = (long)kLaneCTAs * sm_count;
   // z chunks: a wave of CTAs lasts about (planes per unit + 1/2) plane times
   // (the prologue); pick the chunking with the fewest plane times in all
   int best_zc = nz;
@@ -524,7 +528,7 @@ bool plan_lane_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
 
 template <bool ANISO, int TSRC, bool COMP>
 static cudaError_t launch_lane_t(const StepArgs& a, const TilePlan& t, cudaStream_t s) {
-  auto k = pf_lane_kernel<kLaneNV, ANISO, TSRC, kLaneTX, kLaneS, COMP>;
+  auto k = pf_lane_kernel<kLaneNV, ANISO, TSRC, kLaneNC, kLaneCTAs, kLaneTX, kLaneS, COMP>;
   static int configured[64] = {0};
   const int dev = device_info().device;
   if (dev < 0 || dev >= 64 || configured[dev] < (int)t.smem) {
@@ -533,7 +537,7 @@ static cudaError_t launch_lane_t(const StepArgs& a, const TilePlan& t, cudaStrea
     if (e != cudaSuccess) return e;
     if (dev >= 0 && dev < 64) configured[dev] = (int)t.smem;
   }
-  k<<<(unsigned)t.units, 256, t.smem, s>>>(a);
+  k<<<(unsigned)t.units, kLaneNC, t.smem, s>>>(a);
   return cudaGetLastError();
 }
 
