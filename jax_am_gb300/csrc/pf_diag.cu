@@ -496,6 +496,210 @@ pf_inspect_kernel(const __grid_constant__ DiagArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// The full record (free energy, per-orientation mass and the inspect metrics)
+// with one lane per cell, for num_oris a multiple of 4 up to 20.  A warp takes
+// 32 consecutive cells at a time: their n floats are contiguous, so it stages
+// them in its shared-memory slice with 16-byte cp.async copies (the next
+// chunk's copies in flight while this one is reduced), then each lane reduces
+// its cell's orientations in order: sum eta^2, sum eta^4, the gradient energy
+// against the forward neighbours (x + 1 from the staged chunk where it is in
+// it, y + 1 and z + 1 from L2), the argmax, and the per-orientation mass in
+// the lane's own compensated sums.  No per-cell shuffles.  Per-block partial
+// records as for pf_diag_kernel.
+// ---------------------------------------------------------------------------
+constexpr int kCellWarps = 8;
+constexpr int kCellMaxVec = 5;  // n <= 20 (the per-lane mass sums fit in registers)
+
+template <int NV>  // num_oris = 4 NV
+__global__ void __launch_bounds__(32 * kCellWarps, 2)
+pf_diag_cells_kernel(const __grid_constant__ DiagArgs a) {
+  extern __shared__ float4 s_chunks[];  // per warp: two chunks of 32 cells
+  __shared__ double s_mass[kCellWarps][4 * kCellMaxVec];
+  __shared__ double s_energy[kCellWarps], s_maxT[kCellWarps];
+  __shared__ long long s_cnt[kCellWarps][3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int n = 4 * NV, nv = NV;
+  const int ncell = a.nx * a.ny * a.nz;  // < 2^31 (host checks)
+  const int xy = a.nx * a.ny;
+  const int64_t gsy = a.nx + 2, gsz = (int64_t)(a.ny + 2) * (a.nx + 2);
+  float4* buf0 = s_chunks + (size_t)warp * 2 * 32 * nv;
+  float4* buf1 = buf0 + 32 * nv;
+  const float4* eta4 = reinterpret_cast<const float4*>(a.eta);
+  const int nchunks = (int)(((int64_t)ncell + 31) / 32);
+  const int cstride = gridDim.x * kCellWarps;
+
+  float mh[n], ml[n];  // compensated mass per orientation
+#pragma unroll
+  for (int i = 0; i < n; ++i) mh[i] = ml[i] = 0.f;
+  CSum energy;
+  float maxT = -INFINITY;
+  int changed = 0, liquid = 0, nonfinite = 0;
+
+  auto stage = [&](int chunk, float4* dst) {
+    const int c0 = chunk * 32;
+    const int tot = min(32, ncell - c0) * nv;
+    const float4* src = eta4 + (int64_t)c0 * nv;
+    for (int j = lane; j < tot; j += 32) cp_async<16>(dst + j, src + j);
+  };
+  int ch = blockIdx.x * kCellWarps + warp;
+  if (ch < nchunks) stage(ch, buf0);
+  cp_async_commit();
+  for (int it = 0; ch < nchunks; ch += cstride, ++it) {
+    float4* cur = (it & 1) ? buf1 : buf0;
+    float4* nxt = (it & 1) ? buf0 : buf1;
+    if (ch + cstride < nchunks) stage(ch + cstride, nxt);
+    cp_async_commit();
+    cp_async_wait(1);  // this chunk has landed; the next may stay in flight
+    __syncwarp();
+    const int c0 = ch * 32;
+    const int cells = min(32, ncell - c0);
+    if (lane < cells) {
+      const int c = c0 + lane;
+      const int z = c / xy, r = c - z * xy, y = r / a.nx, x = r - y * a.nx;
+      const int64_t ti = a.T_ghosted ? (int64_t)(z + 1) * gsz + (int64_t)(y + 1) * gsy + x + 1
+                                     : (int64_t)c;
+      const float T = __ldg(a.T + ti);
+      // forward neighbours under the boundary conditions (-1: the cell itself)
+      const int cx = (x + 1 < a.nx) ? c + 1 : (a.bcx ? c - (a.nx - 1) : -1);
+      const int cy = (y + 1 < a.ny) ? c + a.nx : (a.bcy ? c - (a.ny - 1) * a.nx : -1);
+      const int cz = (z + 1 < a.nz) ? c + xy : (a.bcz ? c - (a.nz - 1) * xy : -1);
+      const float4* e = cur + lane * nv;
+      const float4* ex = (cx == c + 1 && lane + 1 < cells) ? cur + (lane + 1) * nv
+                                                            : eta4 + (int64_t)(cx < 0 ? c : cx) * nv;
+      const float4* ey = eta4 + (int64_t)(cy < 0 ? c : cy) * nv;
+      const float4* ez = eta4 + (int64_t)(cz < 0 ? c : cz) * nv;
+      float s2 = 0.f, s4 = 0.f, g2 = 0.f, best = -INFINITY, bad = 0.f;
+      int bi = 0;
+#pragma unroll
+      for (int v = 0; v < nv; ++v) {
+        {
+          const float4 u = e[v];
+          const float4 X = (cx < 0) ? u : ex[v];
+          const float4 Y = (cy < 0) ? u : __ldg(ey + v);
+          const float4 Z = (cz < 0) ? u : __ldg(ez + v);
+          const float uu[4] = {u.x, u.y, u.z, u.w}, xx[4] = {X.x, X.y, X.z, X.w};
+          const float yy[4] = {Y.x, Y.y, Y.z, Y.w}, zz[4] = {Z.x, Z.y, Z.z, Z.w};
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float q = uu[k];
+            const int i = 4 * v + k;
+            bad = fmaf(q, 0.f, bad);  // NaN once any value is non-finite
+            if (q > best) { best = q; bi = i; }
+            {  // mass: compensated sum (TwoSum)
+              const float sum = __fadd_rn(mh[i], q);
+              const float bp = __fsub_rn(sum, mh[i]);
+              const float ap = __fsub_rn(sum, bp);
+              ml[i] = __fadd_rn(ml[i], __fadd_rn(__fsub_rn(mh[i], ap), __fsub_rn(q, bp)));
+              mh[i] = sum;
+            }
+            const float qq = q * q;
+            s2 += qq;
+            s4 = fmaf(qq, qq, s4);
+            const float gx = xx[k] - q, gy = yy[k] - q, gz = zz[k] - q;
+            g2 = fmaf(a.gwx * gx, gx, fmaf(a.gwy * gy, gy, fmaf(a.gwz * gz, gz, g2)));
+          }
+        }
+      }
+      if (isnan(bad)) {  // a non-finite value: np.argmax's rules (first NaN wins) and the count
+        const float* ef = reinterpret_cast<const float*>(e);
+        best = -INFINITY;
+        bi = 1 << 30;
+        for (int i = 0; i < n; ++i) {
+          const float q = ef[i];
+          if (!isfinite(q)) ++nonfinite;
+          if (argmax_better(q, i, best, bi)) { best = q; bi = i; }
+        }
+      }
+      // 1 - zeta of allen_cahn.py:56-57, as pf_diag_kernel
+      const float Tc = fminf(T, 2000.f);
+      const float om = isnan(T) ? T : (Tc == a.tl_eq ? 0.5f : (Tc >= a.tl_ge ? 1.f : 0.f));
+      const float f_loc =
+          a.m_g * ((0.25f * s4 - 0.5f * s2) + fmaf(s2, s2, -s4) + om * om * s2);
+      energy.add((f_loc + g2) * a.vol);
+      if (T >= a.tl_ge) ++liquid;
+      if (T > maxT || isnan(T)) maxT = isnan(maxT) ? maxT : T;
+      if (a.argmax_out) a.argmax_out[c] = bi;
+      if (a.argmax0 && __ldg(a.argmax0 + c) != bi) ++changed;
+    }
+    __syncwarp();  // this buffer is restaged in the next iteration but one
+  }
+  cp_async_wait(0);
+
+  // ---- block reduction (fixed order): lanes by butterflies, then warps in order
+  double en = energy.value(), mt = (double)maxT;
+  long long k0 = changed, k1 = liquid, k2 = nonfinite;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    en += __shfl_xor_sync(0xffffffffu, en, o);
+    const double om = __shfl_xor_sync(0xffffffffu, mt, o);
+    if (om > mt || isnan(om)) mt = isnan(mt) ? mt : om;
+    k0 += __shfl_xor_sync(0xffffffffu, k0, o);
+    k1 += __shfl_xor_sync(0xffffffffu, k1, o);
+    k2 += __shfl_xor_sync(0xffffffffu, k2, o);
+  }
+#pragma unroll
+  for (int i = 0; i < n; ++i) {
+    {
+      double m = (double)mh[i] + (double)ml[i];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+      if (lane == 0) s_mass[warp][i] = m;
+    }
+  }
+  if (lane == 0) {
+    s_energy[warp] = en;
+    s_maxT[warp] = mt;
+    s_cnt[warp][0] = k0;
+    s_cnt[warp][1] = k1;
+    s_cnt[warp][2] = k2;
+  }
+  __syncthreads();
+  DiagPartial* out = a.partials + blockIdx.x;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double sm = 0.0;
+    for (int w = 0; w < kCellWarps; ++w) sm += s_mass[w][i];
+    out->mass[i] = sm;
+  }
+  if (threadIdx.x == 0) {
+    double e2 = 0.0, t2 = -INFINITY;
+    long long d0 = 0, d1 = 0, d2 = 0;
+    for (int w = 0; w < kCellWarps; ++w) {
+      e2 += s_energy[w];
+      if (s_maxT[w] > t2 || isnan(s_maxT[w])) t2 = isnan(t2) ? t2 : s_maxT[w];
+      d0 += s_cnt[w][0];
+      d1 += s_cnt[w][1];
+      d2 += s_cnt[w][2];
+    }
+    out->energy = e2;
+    out->max_T = t2;
+    out->changed = d0;
+    out->liquid = d1;
+    out->nonfinite = d2;
+  }
+}
+
+template <int NV>
+static cudaError_t launch_diag_cells_t(const DiagArgs& a, int nb, size_t smem, cudaStream_t s) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(pf_diag_cells_kernel<NV>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  pf_diag_cells_kernel<NV><<<nb, 32 * kCellWarps, smem, s>>>(a);
+  return cudaSuccess;
+}
+
+static cudaError_t launch_diag_cells(const DiagArgs& a, int nb, size_t smem, cudaStream_t s) {
+  switch (a.n / 4) {
+    case 1: return launch_diag_cells_t<1>(a, nb, smem, s);
+    case 2: return launch_diag_cells_t<2>(a, nb, smem, s);
+    case 3: return launch_diag_cells_t<3>(a, nb, smem, s);
+    case 4: return launch_diag_cells_t<4>(a, nb, smem, s);
+    default: return launch_diag_cells_t<5>(a, nb, smem, s);
+  }
+}
+
 int launch_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_ghosted,
                 const int32_t* argmax0, int32_t* argmax_out, void* scratch,
                 pfg_diag* out, cudaStream_t s, bool full = true) {
@@ -537,6 +741,15 @@ int launch_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_
     }
     if (a.n % 4 == 0) pf_inspect_kernel<true><<<nb, 32 * w, smem, s>>>(a);
     else pf_inspect_kernel<false><<<nb, 32 * w, smem, s>>>(a);
+  } else if (a.n % 4 == 0 && a.n <= 4 * kCellMaxVec) {
+    // the lane-per-cell record: no more blocks than partial records or than
+    // chunks of 32 cells per warp
+    const long long nchunks = ((long long)a.nx * a.ny * a.nz + 31) / 32;
+    const long long need = (nchunks + kCellWarps - 1) / kCellWarps;
+    nb = (int)(need < nb ? (need < 1 ? 1 : need) : nb);
+    const size_t smem = (size_t)kCellWarps * 2 * 32 * a.n * sizeof(float);
+    cudaError_t e = launch_diag_cells(a, nb, smem, s);
+    if (e != cudaSuccess) return record_cuda(e);
   } else switch (diag_group(a.n)) {
     case 1: launch_diag_g<1>(a, nb, s); break;
     case 2: launch_diag_g<2>(a, nb, s); break;

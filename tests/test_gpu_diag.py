@@ -22,7 +22,10 @@ def _built():
 @pytest.mark.parametrize("shape,n,bc", [((9, 7, 5), 5, None), ((17, 13, 6), 20, "periodic"),
                                         ((4, 4, 4), 33, None), ((31, 2, 3), 64, None),
                                         ((64, 48, 40), 20, None), ((50, 40, 30), 7, "periodic"),
-                                        ((2, 1, 1), 1, None), ((3, 1, 2), 12, None)])
+                                        ((2, 1, 1), 1, None), ((3, 1, 2), 12, None),
+                                        ((10, 9, 8), 4, ("periodic", "neumann", "periodic")),
+                                        ((33, 5, 7), 8, None), ((40, 17, 3), 16, "periodic"),
+                                        ((1, 1, 37), 20, None), ((90, 70, 20), 20, "periodic")])
 def test_diag_vs_oracle(shape, n, bc):
     from jax_am_gb300.phase_field.allen_cahn import PFSolver
     poly, eta, T, pf_args, oargs, obc = pf_case(shape, n, 0.0, seed=12, bc=bc)
@@ -120,3 +123,28 @@ def test_inspect_async_is_ordered_before_later_steps():
         assert got[k] == ref[k], k
     assert later["max_T"] != ref["max_T"]  # the later state differs
     assert pend.done()
+
+
+@pytest.mark.parametrize("n", [20, 12])
+def test_diag_non_finite_values(n):
+    """The full record with NaN and infinity in eta (lane-per-cell path for
+    n <= 20): the count of non-finite values and np.argmax's rules (the first
+    NaN wins; infinity is a maximum)."""
+    from jax_am_gb300.phase_field.allen_cahn import PFSolver
+    poly, eta, T, pf_args, oargs, obc = pf_case((21, 11, 5), n, 0.0, seed=14)
+    s = PFSolver(pf_args, poly)
+    eta = eta.copy()
+    eta[3, 5] = np.nan
+    eta[3, 2] = np.nan
+    eta[40, 1] = np.inf
+    eta[77, n - 1] = -np.inf
+    # eta0 = eta: the record's own argmax must equal the reference argmax of
+    # eta0 in every cell, NaN and infinity cells included
+    d = s.diagnostics(eta, T, eta)
+    assert d["n_nonfinite"] == 4
+    assert d["n_ori_changed"] == 0
+    got = s.argmax(torch.tensor(eta, dtype=torch.float32, device="cuda")).cpu().numpy()
+    np.testing.assert_array_equal(got, np.argmax(eta.astype(np.float32), axis=1))
+    m = O.inspect(np.nan_to_num(eta), eta, T, oargs["T_liquidus"])
+    assert d["max_T"] == m["max_T"]
+
