@@ -210,7 +210,11 @@ int pfg_device_error(int clear);
  * (256: two CTAs per SM; 512: one larger CTA per SM), 6 = cells per thread of
  * the CFD solver's kernels (1..16, default 4), 7 = 1 to run the TMA-fed
  * kernel's compile-time plans (pfg_fixed_plan) through its run-time-plan
- * instance instead.  Process-wide; the stencil
+ * instance instead, 8 = the wait probe (cycles; 0 = off): each CTA of the
+ * TMA-fed and cell-per-lane kernels first waits that long on a barrier that
+ * nothing completes, so the launch takes its timeout path (the CTA waits for
+ * its copies in flight and returns; PFG_ERR_TIMEOUT in pfg_device_error)
+ * without any fault; its output is then invalid.  Process-wide; the stencil
  * steps' results do not change; the CFD solver's dot products are summed in
  * another order (float64 rounding only). */
 int pfg_tune(int key, int value);
@@ -302,7 +306,8 @@ int pfg_heat_pf_step(const pfg_pf_params* p, const pfg_heat_params* h,
  * temperature is far from ambient and on every domain face.  A float32
  * temperature rounds to ~1e-3 K per step at 1e4 K and drifts from a
  * float64 run by ~1e-2 K over 2000 steps of the laser-track workload; the
- * compensated one stays within ~1e-5 K.  The phase field reads Tg.
+ * compensated one stays within ~2e-6 K (1.1e-6 K measured over those 2000
+ * steps).  The phase field reads Tg.
  * Available for the cell-per-lane kernel (num_oris = 20, see
  * pfg_heat_pf_step_comp_supported); otherwise PFG_ERR_PARAM.  Tg_in/Tg_out
  * and Tlo_in/Tlo_out must not alias.  Same reference functions as

@@ -569,7 +569,7 @@ pf_diag_cells_kernel(const __grid_constant__ DiagArgs a) {
                                                             : eta4 + (int64_t)(cx < 0 ? c : cx) * nv;
       const float4* ey = eta4 + (int64_t)(cy < 0 ? c : cy) * nv;
       const float4* ez = eta4 + (int64_t)(cz < 0 ? c : cz) * nv;
-      float s2 = 0.f, s4 = 0.f, g2 = 0.f, best = -INFINITY, bad = 0.f;
+      float s2 = 0.f, s4 = 0.f, gxx = 0.f, gyy = 0.f, gzz = 0.f, best = -INFINITY;
       int bi = 0;
 #pragma unroll
       for (int v = 0; v < nv; ++v) {
@@ -584,7 +584,6 @@ pf_diag_cells_kernel(const __grid_constant__ DiagArgs a) {
           for (int k = 0; k < 4; ++k) {
             const float q = uu[k];
             const int i = 4 * v + k;
-            bad = fmaf(q, 0.f, bad);  // NaN once any value is non-finite
             if (q > best) { best = q; bi = i; }
             {  // mass: compensated sum (TwoSum)
               const float sum = __fadd_rn(mh[i], q);
@@ -597,11 +596,18 @@ pf_diag_cells_kernel(const __grid_constant__ DiagArgs a) {
             s2 += qq;
             s4 = fmaf(qq, qq, s4);
             const float gx = xx[k] - q, gy = yy[k] - q, gz = zz[k] - q;
-            g2 = fmaf(a.gwx * gx, gx, fmaf(a.gwy * gy, gy, fmaf(a.gwz * gz, gz, g2)));
+            gxx = fmaf(gx, gx, gxx);
+            gyy = fmaf(gy, gy, gyy);
+            gzz = fmaf(gz, gz, gzz);
           }
         }
       }
-      if (isnan(bad)) {  // a non-finite value: np.argmax's rules (first NaN wins) and the count
+      const float g2 = fmaf(a.gwx, gxx, fmaf(a.gwy, gyy, a.gwz * gzz));
+      // A non-finite value makes the sum of squares non-finite (so can a
+      // finite value above 2^64; the exact pass below then finds no
+      // non-finite value and the same argmax): np.argmax's rules (the first
+      // NaN wins) and the count
+      if (!isfinite(s2)) {
         const float* ef = reinterpret_cast<const float*>(e);
         best = -INFINITY;
         bi = 1 << 30;
