@@ -591,6 +591,13 @@ def profile_run(args):
     from jax_am_gb300 import _lib
     solver, g, path, poly = build_case(dict(WORKLOAD, num_oris=args.profile_oris))
     run = HeatPFRun(solver, g, path)
+    if args.state_in:  # a state saved by an earlier --state-out run
+        st = torch.load(args.state_in)
+        run.eta[run.cur].copy_(st["eta"])
+        run.Tg[run.cur].copy_(st["Tg"])
+        if run.compensated:
+            run.Tl[run.cur].copy_(st["Tl"])
+        run.clk[run.cur].copy_(st["clk"])
     run.run(args.warmup, graph=False)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -598,6 +605,10 @@ def profile_run(args):
     run.run(args.steps, graph=False)
     e1.record()
     torch.cuda.synchronize()
+    if args.state_out:
+        torch.save({"eta": run.eta[run.cur].cpu(), "Tg": run.Tg[run.cur].cpu(),
+                    "Tl": run.Tl[run.cur].cpu() if run.compensated else None,
+                    "clk": run.clk[run.cur].cpu()}, args.state_out)
     print(json.dumps({"profile": True, "ms_per_step": e0.elapsed_time(e1) / args.steps,
                       "plan": _lib.describe_plan(solver.params)}), flush=True)
 
@@ -640,6 +651,11 @@ def main():
                     help="eager launches only (warmup then steps), for ncu captures")
     ap.add_argument("--profile-oris", type=int, default=WORKLOAD["num_oris"],
                     help="orientation count of the --profile workload")
+    ap.add_argument("--state-out", default=None,
+                    help="--profile: save the state after the run (eta, T, clock) to this file")
+    ap.add_argument("--state-in", default=None,
+                    help="--profile: start from a state saved by --state-out (a late state "
+                         "with few launches before an ncu capture)")
     ap.add_argument("--profile-inspect", action="store_true",
                     help="the inspect_sol metrics kernels only, on the laser-track state "
                          "after --warmup steps (50 timed records each), for ncu captures")

@@ -415,17 +415,24 @@ __global__ void __launch_bounds__(NC, MINB) pf_lane_kernel(const __grid_constant
         // zero (gradient, Laplacian and local term vanish, and the update of
         // +0.0 is +0.0 with finite coefficients), so the warp skips its
         // arithmetic.  Grain interiors and the far side of an interface are
-        // such zeros.
-        unsigned bits = 0u;
-        {
-          const float4 w[7] = {cc[v], zm[v], xm, xp, ym, yp, zp};
+        // such zeros.  The cells' own vectors (in registers) are tested
+        // first; the neighbours only when those are zero across the warp.
+        const unsigned own_bits =
+            __float_as_uint(cc[v].x) | __float_as_uint(cc[v].y) | __float_as_uint(cc[v].z) |
+            __float_as_uint(cc[v].w) | __float_as_uint(zm[v].x) | __float_as_uint(zm[v].y) |
+            __float_as_uint(zm[v].z) | __float_as_uint(zm[v].w);
+        bool work = !kfinite || __any_sync(0xffffffffu, own_bits != 0u);
+        if (!work) {
+          unsigned bits = 0u;
+          const float4 w[5] = {xm, xp, ym, yp, zp};
 #pragma unroll
-          for (int i = 0; i < 7; ++i)
+          for (int i = 0; i < 5; ++i)
             bits |= __float_as_uint(w[i].x) | __float_as_uint(w[i].y) |
                     __float_as_uint(w[i].z) | __float_as_uint(w[i].w);
+          work = __any_sync(0xffffffffu, bits != 0u);
         }
         float r[4] = {0.f, 0.f, 0.f, 0.f};
-        if (!kfinite || __any_sync(0xffffffffu, bits != 0u))
+        if (work)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int o = 4 * v + q;  // orientation

@@ -185,7 +185,7 @@ class HeatPFRun(_GraphRun):
     ``compensated`` (default: wherever the step kernel supports it, i.e.
     num_oris = 20) keeps the temperature as two float32 fields whose sum is
     T (``pfg_heat_pf_step_comp``): a 2000-step laser run then tracks a
-    float64 run to ~1e-5 K instead of ~1e-2 K (plus O(1 K) where a cell near
+    float64 run to ~1e-6 K instead of ~1e-2 K (plus O(1 K) where a cell near
     the latent-heat or liquidus switch takes the other branch).
     ``T_ghosted`` is the float32 temperature (the high part);
     ``T_ghosted_f64`` the full value."""
