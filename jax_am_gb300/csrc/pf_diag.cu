@@ -40,8 +40,26 @@ struct DiagPartial {
   double mass[PFG_MAX_ORIS];
 };
 
+// n / d for 0 <= n < 2^31 as (umulhi(n, m) + n) >> s, with s = ceil(log2 d)
+// and m = floor(2^32 (2^s - d) / d) + 1 (Granlund and Montgomery's
+// round-up multiplier; the sum stays below 2^32 because n < 2^31).
+struct FastDiv {
+  uint32_t m;
+  int s;
+};
+static FastDiv make_fastdiv(int d) {
+  int s = 0;
+  while ((1LL << s) < (long long)d) ++s;
+  const uint64_t m = ((uint64_t)1 << 32) * (((uint64_t)1 << s) - (uint64_t)d) / (uint64_t)d + 1;
+  return FastDiv{(uint32_t)m, s};
+}
+__device__ __forceinline__ int fast_div(int n, FastDiv f) {
+  return (int)((__umulhi((uint32_t)n, f.m) + (uint32_t)n) >> f.s);
+}
+
 struct DiagArgs {
   int nx, ny, nz, n;
+  FastDiv div_x, div_xy;  // by nx and by nx * ny
   int bcx, bcy, bcz;
   int T_ghosted;
   float gwx, gwy, gwz;  // kappa_g / 2 / h_d^2: the gradient energy weight per axis
@@ -536,11 +554,24 @@ pf_diag_cells_kernel(const __grid_constant__ DiagArgs a) {
   float maxT = -INFINITY;
   int changed = 0, liquid = 0, nonfinite = 0;
 
+  // the chunk's y + 1 and z + 1 neighbours are the 32 cells nx and nx * ny
+  // further on: their 128-byte lines (at most 21 for n <= 20) are prefetched
+  // into L1 one chunk ahead, so the lanes' 16-byte loads of them hit L1
+  const int64_t nbytes = (int64_t)ncell * n * 4;
+  const char* eta_b = reinterpret_cast<const char*>(a.eta);
+  auto prefetch_span = [&](int64_t cell0) {
+    const int64_t b0 = (cell0 * n * 4) & ~(int64_t)127;
+    const int64_t b = b0 + (int64_t)lane * 128;
+    if (lane * 128 < 32 * n * 4 + 128 && b < nbytes)
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(eta_b + b));
+  };
   auto stage = [&](int chunk, float4* dst) {
     const int c0 = chunk * 32;
     const int tot = min(32, ncell - c0) * nv;
     const float4* src = eta4 + (int64_t)c0 * nv;
     for (int j = lane; j < tot; j += 32) cp_async<16>(dst + j, src + j);
+    prefetch_span((int64_t)c0 + a.nx);
+    prefetch_span((int64_t)c0 + xy);
   };
   int ch = blockIdx.x * kCellWarps + warp;
   if (ch < nchunks) stage(ch, buf0);
@@ -556,7 +587,8 @@ pf_diag_cells_kernel(const __grid_constant__ DiagArgs a) {
     const int cells = min(32, ncell - c0);
     if (lane < cells) {
       const int c = c0 + lane;
-      const int z = c / xy, r = c - z * xy, y = r / a.nx, x = r - y * a.nx;
+      const int z = fast_div(c, a.div_xy), r = c - z * xy, y = fast_div(r, a.div_x);
+      const int x = r - y * a.nx;
       const int64_t ti = a.T_ghosted ? (int64_t)(z + 1) * gsz + (int64_t)(y + 1) * gsy + x + 1
                                      : (int64_t)c;
       const float T = __ldg(a.T + ti);
@@ -713,6 +745,8 @@ int launch_diag(const pfg_pf_params* p, const float* eta, const float* T, int T_
   if ((int64_t)p->nx * p->ny * p->nz >= ((int64_t)1 << 31)) return PFG_ERR_SHAPE;
   DiagArgs a{};
   a.nx = p->nx; a.ny = p->ny; a.nz = p->nz; a.n = p->num_oris;
+  a.div_x = make_fastdiv(p->nx);
+  a.div_xy = make_fastdiv(p->nx * p->ny);
   a.bcx = p->bc_x; a.bcy = p->bc_y; a.bcz = p->bc_z;
   a.T_ghosted = T_ghosted;
   a.gwx = (float)(0.5 * (double)p->kappa_g / ((double)p->h_x * p->h_x));
