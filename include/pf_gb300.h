@@ -307,9 +307,13 @@ int pfg_heat_pf_step(const pfg_pf_params* p, const pfg_heat_params* h,
  * temperature rounds to ~1e-3 K per step at 1e4 K and drifts from a
  * float64 run by ~1e-2 K over 2000 steps of the laser-track workload; the
  * compensated one stays within ~2e-6 K (1.1e-6 K measured over those 2000
- * steps).  The phase field reads Tg.
- * Available for the cell-per-lane kernel (num_oris = 20, see
- * pfg_heat_pf_step_comp_supported); otherwise PFG_ERR_PARAM.  Tg_in/Tg_out
+ * steps).  The phase field reads Tg, and zeta the exact pair.
+ * The cell-per-lane kernel (num_oris = 20) evaluates the heat update inside
+ * the stencil; where the TMA-fed kernel runs instead (num_oris a multiple of
+ * 4, or even with even nx and Neumann x faces) the step is two launches: the
+ * compensated heat update, then the phase field with the start-of-step
+ * pair (both read only the old state; 16 more bytes of traffic per cell).
+ * Otherwise PFG_ERR_PARAM (see pfg_heat_pf_step_comp_supported).  Tg_in/Tg_out
  * and Tlo_in/Tlo_out must not alias.  Same reference functions as
  * pfg_heat_pf_step (allen_cahn.py:106-114, gamma.py:9-61). */
 int pfg_heat_pf_step_comp(const pfg_pf_params* p, const pfg_heat_params* h,

@@ -736,8 +736,15 @@ extern "C" int pfg_heat_pf_step_comp_supported(const pfg_pf_params* p) {
   int st = check_pf_params(p);
   if (st) return -st;
   if (!device_info().ok) return -PFG_ERR_NO_DEVICE;
+  if ((int64_t)(p->nx + 2) * (p->ny + 2) * (p->nz + 2) >= ((int64_t)1 << 31)) return 0;
+  const DeviceInfo& d = device_info();
   TilePlan t;
-  return (g_kernel_variant == 0 && plan_lane(*p, &t)) ? 1 : 0;
+  const int v = g_kernel_variant;
+  if (v == 0 && plan_lane(*p, &t)) return 1;
+  return ((v == 0 || v == 3) && plan_tma_tiles(p->nx, p->ny, p->nz, p->num_oris, p->bc_x,
+                                               d.sm_count, d.smem_per_sm, &t))
+             ? 1
+             : 0;
 }
 
 extern "C" int pfg_heat_pf_step_comp(const pfg_pf_params* p, const pfg_heat_params* h,
@@ -757,8 +764,11 @@ extern "C" int pfg_heat_pf_step_comp(const pfg_pf_params* p, const pfg_heat_para
   if (clk_in == clk_out || Tg_in == Tg_out || Tlo_in == Tlo_out) return PFG_ERR_PARAM;
   if (!aligned16(eta_in) || !aligned16(eta_out)) return PFG_ERR_ALIGN;
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
-  TilePlan t;
-  if (g_kernel_variant != 0 || !plan_lane(*p, &t)) return PFG_ERR_PARAM;
+  // ghosted offsets are 32-bit in the compensated kernels
+  if ((int64_t)(p->nx + 2) * (p->ny + 2) * (p->nz + 2) >= ((int64_t)1 << 31))
+    return PFG_ERR_SHAPE;
+  const DeviceInfo& d = device_info();
+  const int v = g_kernel_variant;
   StepArgs a{};
   a.eta_in = eta_in; a.eta_out = eta_out; a.T = Tg_in; a.T_out = Tg_out;
   a.T_lo = Tlo_in; a.T_lo_out = Tlo_out;
@@ -766,7 +776,22 @@ extern "C" int pfg_heat_pf_step_comp(const pfg_pf_params* p, const pfg_heat_para
   a.hc = make_heat_consts(*h);
   a.hd = make_heat_df(*h, dt);
   a.hp = *h;
-  fill_common(a, *p, t, dt);
-  a.cpw = t.cpw; a.wx = t.wx; a.rpw = t.rpw;
-  return record_cuda(launch_lane_kernel<kTHeat>(a, t, static_cast<cudaStream_t>(stream)));
+  const cudaStream_t cs = static_cast<cudaStream_t>(stream);
+  TilePlan t;
+  if (v == 0 && plan_lane(*p, &t)) {  // the heat update inside the stencil
+    fill_common(a, *p, t, dt);
+    a.cpw = t.cpw; a.wx = t.wx; a.rpw = t.rpw;
+    return record_cuda(launch_lane_kernel<kTHeat>(a, t, cs));
+  }
+  if ((v == 0 || v == 3) &&
+      plan_tma_tiles(p->nx, p->ny, p->nz, p->num_oris, p->bc_x, d.sm_count, d.smem_per_sm, &t)) {
+    // the compensated heat update in its own kernel, then the phase field
+    // with the start-of-step pair (both read only the old state)
+    fill_common(a, *p, t, dt);
+    a.cpw = t.cpw; a.wx = t.wx; a.rpw = t.rpw;
+    cudaError_t e = launch_heat_comp(a, cs);
+    if (e != cudaSuccess) return record_cuda(e);
+    return record_cuda(launch_tma_kernel<kTHeat>(a, t, cs));
+  }
+  return PFG_ERR_PARAM;
 }

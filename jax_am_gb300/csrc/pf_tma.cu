@@ -359,6 +359,13 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
         const float Tp = __ldg(a.T + ti), Tf = __ldg(a.T2 + ti);
         tc = temp_coefficients_fast(a.pc, w_past * Tp + (1.f - w_past) * Tf, a.dt);
       }
+      else if constexpr (TSRC == kTHeat) {
+        // compensated state (a.T_lo set): zeta from the exact pair
+        tc = a.T_lo ? temp_coefficients_pair(
+                          a.pc, ts[c_toff[q]],
+                          __ldg(a.T_lo + (int64_t)(pz + 1) * gsz + c_g[q]), a.dt)
+                    : temp_coefficients_fast(a.pc, ts[c_toff[q]], a.dt);
+      }
       else tc = temp_coefficients_fast(a.pc, ts[c_toff[q]], a.dt);
       cb[c_cc[q]] = tma_fold(a.pc, tc, s0 + s1);
     }
@@ -415,8 +422,10 @@ pf_tma_kernel(const __grid_constant__ StepArgs a) {
           a.T_out[idx] = Tn;
         }
       };
-      // CTA-uniform: no cell of this tile plane touches a domain face
-      if (tile_inner && z > 0 && z < a.nz - 1) heat_cells(std::false_type{});
+      // CTA-uniform: no cell of this tile plane touches a domain face.  With a
+      // compensated state the heat update has run in its own kernel.
+      if (a.T_lo) {
+      } else if (tile_inner && z > 0 && z < a.nz - 1) heat_cells(std::false_type{});
       else heat_cells(std::true_type{});
     }
     if (z + 1 < ze) cell_coefs(s_next, (m + 1) & 1, z + 1);

@@ -65,6 +65,10 @@ bool plan_lane_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
                      int max_smem_per_block, int zchunks_override, TilePlan* out);
 template <int TSRC>
 cudaError_t launch_lane_kernel(const StepArgs& a, const TilePlan& t, cudaStream_t s);
+// Compensated heat step alone (heat_comp.cu): a.T, a.T_lo -> a.T_out,
+// a.T_lo_out, the beam at mid-step from a.clk_in (the fused compensated step
+// of the kernels other than the cell-per-lane one).
+cudaError_t launch_heat_comp(const StepArgs& a, cudaStream_t s);
 // The device error flags (PFG_ERR_TIMEOUT after a bounded wait ran out) of
 // the TMA-fed and the cell-per-lane kernels, or a negative pfg_status if one
 // cannot be read; clear != 0 resets it.

@@ -182,9 +182,10 @@ def raster(tracks, speed, power, x_start, x_end, t_start=0.0):
 class HeatPFRun(_GraphRun):
     """Fused explicit heat + phase-field run with a tool-path laser.
 
-    ``compensated`` (default: wherever the step kernel supports it, i.e.
-    num_oris = 20) keeps the temperature as two float32 fields whose sum is
-    T (``pfg_heat_pf_step_comp``): a 2000-step laser run then tracks a
+    ``compensated`` (default: wherever the step kernels support it: the
+    cell-per-lane kernel (num_oris = 20) and the TMA-fed kernel) keeps the
+    temperature as two float32 fields whose sum is T
+    (``pfg_heat_pf_step_comp``): a 2000-step laser run then tracks a
     float64 run to ~1e-6 K instead of ~1e-2 K (plus O(1 K) where a cell near
     the latent-heat or liquidus switch takes the other branch).
     ``T_ghosted`` is the float32 temperature (the high part);
@@ -212,8 +213,9 @@ class HeatPFRun(_GraphRun):
         if compensated is None:
             compensated = supported
         elif compensated and not supported:
-            raise ValueError("the compensated fused step needs the cell-per-lane kernel "
-                             "(num_oris = 20)")
+            raise ValueError("the compensated fused step needs the cell-per-lane or the "
+                             "TMA-fed step kernel (num_oris = 20, or a multiple of 4, or even "
+                             "with even Nx and Neumann x faces)")
         self.compensated = bool(compensated)
         self.Tl = [torch.zeros_like(Tg), torch.zeros_like(Tg)] if self.compensated else None
         self.set_time(t0)

@@ -61,12 +61,15 @@ def _compare(name, e_gpu, e_ref, T_gpu=None, T_ref=None):
         assert t_err <= T_TOL
 
 
-def _laser_case(shape, n, grains, aniso, path, steps, seed, name, chunk=None, graph=True):
+def _laser_case(shape, n, grains, aniso, path, steps, seed, name, chunk=None, graph=True,
+                compensated=None):
     """Fused laser run of ``steps`` steps on the GPU against the float64
     PyTorch restatement; returns the highest interior temperature the float64
     run reached in any step (so that callers can require the melt branch:
     T >= T_liquidus switches zeta and the liquid front).  ``chunk``: evaluate
-    the float64 phase field that many z planes at a time (large grids)."""
+    the float64 phase field that many z planes at a time (large grids).
+    ``compensated``: True / False to require that temperature state (None:
+    the run's default)."""
     from jax_am_gb300.phase_field.allen_cahn import PFSolver
     from jax_am_gb300.phase_field.utils import Field
     from jax_am_gb300.runner import HeatPFRun
@@ -77,7 +80,9 @@ def _laser_case(shape, n, grains, aniso, path, steps, seed, name, chunk=None, gr
     poly = Field(pf_args, seed=seed)
     s = PFSolver(pf_args, poly)
     g = gamma_args()
-    run = HeatPFRun(s, g, path)
+    run = HeatPFRun(s, g, path, compensated=compensated)
+    if compensated is not None:
+        assert run.compensated == compensated
     dt = float(np.float32(run.dt))
     run.run(steps, graph=graph)
     a = _oracle_args(pf_args, poly)
