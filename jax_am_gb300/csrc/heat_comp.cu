@@ -55,14 +55,30 @@ heat_comp_kernel(const __grid_constant__ StepArgs a) {
   float Tzm = __ldg(Th + idx - gsz), Lzm = __ldg(Tl + idx - gsz);
   float Tc = __ldg(Th + idx), Lc = __ldg(Tl + idx);
   const bool side = gx == 0 || gx == nx - 1 || gy == 0 || gy == ny - 1;
+  // the next plane's loads are issued one plane ahead (the loop body is not
+  // unrolled: the double-float update is long)
+  float q[10];
+  auto load_plane = [&](int i) {
+    q[0] = __ldg(Th + i + gsz);
+    q[1] = __ldg(Tl + i + gsz);
+    q[2] = __ldg(Th + i - 1);
+    q[3] = __ldg(Th + i + 1);
+    q[4] = __ldg(Th + i - gsy);
+    q[5] = __ldg(Th + i + gsy);
+    q[6] = __ldg(Tl + i - 1);
+    q[7] = __ldg(Tl + i + 1);
+    q[8] = __ldg(Tl + i - gsy);
+    q[9] = __ldg(Tl + i + gsy);
+  };
+  load_plane(idx);
+#pragma unroll 1
   for (int z = z0; z < z1; ++z, idx += gsz) {
-    const float Tzp = __ldg(Th + idx + gsz), Lzp = __ldg(Tl + idx + gsz);
-    const float Txm = __ldg(Th + idx - 1), Txp = __ldg(Th + idx + 1);
-    const float Tym = __ldg(Th + idx - gsy), Typ = __ldg(Th + idx + gsy);
+    const float Tzp = q[0], Lzp = q[1];
+    const float Txm = q[2], Txp = q[3], Tym = q[4], Typ = q[5];
     const DF c{Tc, Lc};
-    DF n[6] = {DF{Txm, __ldg(Tl + idx - 1)},   DF{Txp, __ldg(Tl + idx + 1)},
-               DF{Tym, __ldg(Tl + idx - gsy)}, DF{Typ, __ldg(Tl + idx + gsy)},
-               DF{Tzm, Lzm},                   DF{Tzp, Lzp}};
+    DF n[6] = {DF{Txm, q[6]}, DF{Txp, q[7]}, DF{Tym, q[8]}, DF{Typ, q[9]}, DF{Tzm, Lzm},
+               DF{Tzp, Lzp}};
+    if (z + 1 < z1) load_plane(idx + gsz);  // block-uniform
     const bool on_face = side || z == 0 || z == nz - 1;
     const float tmax =
         fmaxf(fmaxf(fmaxf(Tc, Txm), fmaxf(Txp, Tym)), fmaxf(fmaxf(Typ, Tzm), Tzp));
