@@ -26,6 +26,7 @@
 
 #include "pfg_host.h"
 #include "pfg_step.cuh"
+#include "pfg_tma.cuh"
 #include "pfg_warp.cuh"
 
 namespace pfg {
@@ -36,7 +37,8 @@ struct BatchJobDev {
   double t0;
   long long base_step, target_steps;
   long long unit_begin;
-  int units, vec, aniso, pad;
+  int units, vec, aniso;
+  int body;  // 1: the TMA-fed unit body (num_oris % 4 == 0), 0: warp-per-cells
 };
 
 struct BatchHeader {
@@ -48,17 +50,20 @@ struct BatchHeader {
 };
 static_assert(sizeof(BatchHeader) % 16 == 0, "job records follow the header 16-byte aligned");
 
-constexpr int kBatchVersion = 1;
+constexpr int kBatchVersion = 2;
+
+__device__ int g_batch_device_error = 0;  // PFG_ERR_TIMEOUT once a bounded wait ran out
 
 __global__ void __launch_bounds__(kThreads, 2)
 pf_batch_kernel(BatchHeader* __restrict__ hdr, int k) {
-  extern __shared__ __align__(16) float smem[];
+  extern __shared__ __align__(128) float smem[];
   __shared__ __align__(16) StepArgs s_args;
   __shared__ int s_job;
   __shared__ long long s_unit;
   const BatchJobDev* jobs = reinterpret_cast<const BatchJobDev*>(hdr + 1);
   const long long total = hdr->total_units;
   const int nj = hdr->num_jobs;
+  bool tma_barriers = false;  // this CTA's TMA-unit barriers are initialised
   for (;;) {
     if (threadIdx.x == 0) {
       const long long u = (long long)atomicAdd(&hdr->next_unit, 1ULL);
@@ -78,7 +83,20 @@ pf_batch_kernel(BatchHeader* __restrict__ hdr, int k) {
     if (u >= total) break;  // uniform across the CTA
     const BatchJobDev& J = jobs[s_job];
     const long long step = J.base_step + k;
-    if (step < J.target_steps) {  // uniform over the CTA
+    if (step < J.target_steps && J.body == 1) {  // uniform over the CTA
+      // the TMA-fed body reads the job's arguments from the table (L1/L2)
+      const double t0 = J.t0 + (double)step * (double)J.args.dt;
+      const int unit = (int)(u - J.unit_begin);
+      const float* ein = J.eta[step & 1];
+      float* eout = J.eta[(step + 1) & 1];
+      if (J.aniso)
+        tma_unit<true, kTQuench, kThreads, 4, 0, true>(J.args, unit, ein, eout, t0, tma_barriers,
+                                                       &g_batch_device_error);
+      else
+        tma_unit<false, kTQuench, kThreads, 4, 0, true>(J.args, unit, ein, eout, t0, tma_barriers,
+                                                        &g_batch_device_error);
+      tma_barriers = true;
+    } else if (step < J.target_steps) {  // uniform over the CTA
       // the job's arguments into shared memory, then this step's buffers
       const int4* src = reinterpret_cast<const int4*>(&J.args);
       int4* dst = reinterpret_cast<int4*>(&s_args);
@@ -135,6 +153,20 @@ static size_t batch_smem_budget(const DeviceInfo& d) {
 
 using namespace pfg;
 
+namespace pfg {
+int read_batch_device_error(int clear) {
+  int v = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, g_batch_device_error, sizeof(int));
+  if (e != cudaSuccess) return record_cuda(e);
+  if (clear && v) {
+    const int zero = 0;
+    e = cudaMemcpyToSymbol(g_batch_device_error, &zero, sizeof(int));
+    if (e != cudaSuccess) return record_cuda(e);
+  }
+  return v;
+}
+}  // namespace pfg
+
 extern "C" int64_t pfg_batch_table_bytes(int num_jobs) {
   if (num_jobs < 0) return -1;
   return (int64_t)sizeof(BatchHeader) + (int64_t)num_jobs * (int64_t)sizeof(BatchJobDev);
@@ -151,6 +183,7 @@ extern "C" int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* t
   BatchHeader* hdr = static_cast<BatchHeader*>(table);
   BatchJobDev* out = reinterpret_cast<BatchJobDev*>(hdr + 1);
   std::vector<TilePlan> plans((size_t)num_jobs);
+  std::vector<int> bodies((size_t)num_jobs, 0);
   std::vector<std::pair<double, int>> order((size_t)num_jobs);
   for (int j = 0; j < num_jobs; ++j) {
     const pfg_batch_job& J = jobs[j];
@@ -161,10 +194,21 @@ extern "C" int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* t
     if (J.eta[0] == J.eta[1] || J.target_steps < 0 || J.base_step < 0) return PFG_ERR_PARAM;
     TilePlan& t = plans[(size_t)j];
     // tiles chosen for cover and halo only: the batch has units enough to
-    // fill the GPU whatever their count
-    if (!plan_warp_tiles_ex(J.params.nx, J.params.ny, J.params.nz, J.params.num_oris,
-                            d.sm_count, budget, kThreads / 32, 0, 1 << 30, &t))
+    // fill the GPU whatever their count.  num_oris % 4 == 0: the TMA-fed
+    // body (at most two cells per thread in its per-cell pass, 16-byte
+    // vectors, ring barriers in static shared memory)
+    bool tma = false;
+    if (J.params.num_oris % 4 == 0 &&
+        plan_warp_tiles_ex(J.params.nx, J.params.ny, J.params.nz, J.params.num_oris, d.sm_count,
+                           budget - 64, kThreads / 32, 0, 2 * kThreads, &t) &&
+        t.vec == 4 && t.stages <= kTmaMaxStages) {
+      t.rs = kThreads;
+      tma = true;
+    } else if (!plan_warp_tiles_ex(J.params.nx, J.params.ny, J.params.nz, J.params.num_oris,
+                                   d.sm_count, budget, kThreads / 32, 0, 1 << 30, &t)) {
       return PFG_ERR_SHAPE;  // orientation count the warp-per-cells body cannot take
+    }
+    bodies[(size_t)j] = tma ? 1 : 0;
     // units of whole z columns (or 64-plane chunks), so that few halo planes
     // are read twice
     const int zch = std::max(1, (J.params.nz + 63) / 64);
@@ -199,6 +243,7 @@ extern "C" int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* t
     D.units = (int)t.units;
     D.vec = t.vec;
     D.aniso = J.params.anisotropy > 0.f ? 1 : 0;
+    D.body = bodies[(size_t)j];
     units += t.units;
   }
   hdr->num_jobs = num_jobs;

@@ -584,9 +584,11 @@ extern "C" int pfg_device_error(int clear) {
   if (!device_info().ok) return PFG_ERR_NO_DEVICE;
   const int v = read_device_error(clear);
   const int w = read_lane_device_error(clear);
+  const int b = read_batch_device_error(clear);
   if (v < 0) return v;
   if (w < 0) return w;
-  return v ? v : w;
+  if (b < 0) return b;
+  return v ? v : (w ? w : b);
 }
 
 extern "C" int pfg_set_kernel_variant(int variant) {

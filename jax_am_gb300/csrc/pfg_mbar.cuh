@@ -21,6 +21,11 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned by
                "r"(bytes)
                : "memory");
 }
+// Invalidate a barrier whose phases have all completed, so that its memory
+// can be initialised again.
+__device__ __forceinline__ void mbar_inval(uint64_t* bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(smem_addr(bar)) : "memory");
+}
 // Arrive on the barrier once this thread's earlier cp.async copies land
 // (the barrier's expected count includes this arrival).
 __device__ __forceinline__ void cp_async_mbar_arrive_noinc(uint64_t* bar) {

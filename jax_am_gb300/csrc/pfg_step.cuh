@@ -74,6 +74,7 @@ cudaError_t launch_heat_comp(const StepArgs& a, cudaStream_t s);
 // cannot be read; clear != 0 resets it.
 int read_device_error(int clear);
 int read_lane_device_error(int clear);
+int read_batch_device_error(int clear);
 extern int g_tune_zchunks;
 extern long long g_probe_wait;
 

@@ -62,6 +62,27 @@ def test_batch_matches_plain_solver_and_mix_equals_alone():
     assert _lib.device_error() == 0
 
 
+@pytest.mark.parametrize("pad", [True, False], ids=["padded_tma_body", "unpadded_warp_body"])
+def test_batch_bodies_match_plain_solver(pad):
+    """Orientation counts padded to a multiple of 4 run the TMA-fed unit
+    body (persistent CTAs re-initialise its barriers for every unit);
+    unpadded odd counts run the warp-per-cells body; both match the plain
+    per-job solver, and a CTA can take units of both bodies in turn."""
+    from jax_am_gb300 import _lib
+    from jax_am_gb300.serving import BatchServer, run_sequential
+    mix = _mix() + [make_job((36, 20, 12), 16, 33, 6, aniso=0.15)]
+    srv = BatchServer(max_jobs=8, graph_steps=8, pad_oris=pad)
+    for j in mix:
+        srv.submit(j)
+    srv.run(realtime=False)
+    plain = _mix() + [make_job((36, 20, 12), 16, 33, 6, aniso=0.15)]
+    run_sequential(plain, realtime=False)
+    for jb, jp in zip(mix, plain):
+        err = (jb.result - jp.result).abs().max().item()
+        assert err <= ETA_TOL, (jb.cells, jb.num_oris, err)
+    assert _lib.device_error() == 0
+
+
 def test_graph_replay_equals_eager():
     from jax_am_gb300.serving import BatchServer
     res = []
