@@ -51,6 +51,7 @@ struct BatchHeader {
 static_assert(sizeof(BatchHeader) % 16 == 0, "job records follow the header 16-byte aligned");
 
 constexpr int kBatchVersion = 2;
+constexpr int kBatchCachedJobs = 256;  // job tables up to this size are searched in shared memory
 
 __device__ int g_batch_device_error = 0;  // PFG_ERR_TIMEOUT once a bounded wait ran out
 
@@ -60,9 +61,14 @@ pf_batch_kernel(BatchHeader* __restrict__ hdr, int k) {
   __shared__ __align__(16) StepArgs s_args;
   __shared__ int s_job;
   __shared__ long long s_unit;
+  __shared__ int s_begin[kBatchCachedJobs];  // the jobs' first units (host keeps them < 2^31)
   const BatchJobDev* jobs = reinterpret_cast<const BatchJobDev*>(hdr + 1);
   const long long total = hdr->total_units;
   const int nj = hdr->num_jobs;
+  const bool cached = nj <= kBatchCachedJobs;
+  if (cached)
+    for (int i = threadIdx.x; i < nj; i += blockDim.x) s_begin[i] = (int)jobs[i].unit_begin;
+  __syncthreads();
   bool tma_barriers = false;  // this CTA's TMA-unit barriers are initialised
   for (;;) {
     if (threadIdx.x == 0) {
@@ -72,7 +78,7 @@ pf_batch_kernel(BatchHeader* __restrict__ hdr, int k) {
         int lo = 0, hi = nj - 1;  // last job whose first unit is <= u
         while (lo < hi) {
           const int mid = (lo + hi + 1) >> 1;
-          if (jobs[mid].unit_begin <= u) lo = mid;
+          if ((cached ? (long long)s_begin[mid] : jobs[mid].unit_begin) <= u) lo = mid;
           else hi = mid - 1;
         }
         s_job = lo;
@@ -146,7 +152,7 @@ __global__ void pf_batch_advance_kernel(BatchHeader* __restrict__ hdr, int k_ste
 // Dynamic shared memory of every batch launch: two CTAs per SM, less the
 // kernel's static shared memory.
 static size_t batch_smem_budget(const DeviceInfo& d) {
-  return (size_t)d.smem_per_sm / 2 - 2048 - sizeof(StepArgs) - 64;
+  return (size_t)d.smem_per_sm / 2 - 2048 - sizeof(StepArgs) - 64 - kBatchCachedJobs * sizeof(int);
 }
 
 }  // namespace pfg
@@ -246,6 +252,7 @@ extern "C" int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* t
     D.body = bodies[(size_t)j];
     units += t.units;
   }
+  if (units >= ((long long)1 << 31)) return PFG_ERR_CAPACITY;  // unit indices are 32-bit
   hdr->num_jobs = num_jobs;
   hdr->pad = kBatchVersion;
   hdr->total_units = units;
