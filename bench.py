@@ -613,6 +613,45 @@ def profile_run(args):
                       "plan": _lib.describe_plan(solver.params)}), flush=True)
 
 
+def profile_batch(args):
+    """Eager launches of the batched serving kernel: the first 64 jobs of the
+    serving stream admitted at once (about 2 GB resident), ``--warmup``
+    launches, then ``--steps`` timed ones (each advances every job by a
+    step): ``ncu -k regex:pf_batch_kernel -s <warmup> -c 1 python bench.py
+    --profile-batch`` captures the first timed launch."""
+    import __graft_entry__
+    __graft_entry__.build()
+    import ctypes
+    from jax_am_gb300 import _lib
+    from jax_am_gb300.serving import BatchServer
+    from jax_am_gb300.workloads import serving_stream
+    jobs = serving_stream(256, 50.0)[:64]
+    srv = BatchServer(hbm_budget=120e9, max_jobs=64, graph_steps=16)
+    for j in jobs:
+        j.arrival = 0.0
+        srv.submit(j)
+    srv._admit(float("inf"))
+    srv._encode()
+    lib = _lib.load()
+    tab = ctypes.c_void_p(srv.table_dev.data_ptr())
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for k in range(args.warmup):
+        _lib.check(lib.pfg_batch_step(tab, k, s), "pfg_batch_step")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k in range(args.warmup, args.warmup + args.steps):
+        _lib.check(lib.pfg_batch_step(tab, k, s), "pfg_batch_step")
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # eta read and written once per cell and stored orientation (padded)
+    nbytes = sum(j.cells * j._n_store * 8 for j in jobs)
+    print(json.dumps({"profile_batch": True, "jobs": len(jobs), "ms_per_launch": ms,
+                      "bytes_per_launch": nbytes,
+                      "achieved_GBps": nbytes / (ms / 1e3) / 1e9}), flush=True)
+
+
 def profile_cfd(args):
     """``--steps`` eager steps of the CFD driver case (``time_cfd``'s
     workload), each phase in an NVTX range (``AM_3d.energy``,
@@ -656,6 +695,8 @@ def main():
     ap.add_argument("--state-in", default=None,
                     help="--profile: start from a state saved by --state-out (a late state "
                          "with few launches before an ncu capture)")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="eager launches of the batched serving kernel on 64 jobs, for ncu")
     ap.add_argument("--profile-inspect", action="store_true",
                     help="the inspect_sol metrics kernels only, on the laser-track state "
                          "after --warmup steps (50 timed records each), for ncu captures")
@@ -681,6 +722,9 @@ def main():
         return
     if args.profile_cfd:
         profile_cfd(args)
+        return
+    if args.profile_batch:
+        profile_batch(args)
         return
     if args.profile:
         profile_run(args)

@@ -27,21 +27,27 @@ constexpr int kHeatCompChunk = 8;  // cells marched per thread along z
 
 __global__ void __launch_bounds__(256)
 heat_comp_kernel(const __grid_constant__ StepArgs a) {
-  __shared__ float s_beam[5];  // xl, yl, P and the low parts of xl, yl
-  if (threadIdx.x == 0) {
-    // the beam centre and power at mid-step, the centre also as double-float
-    double xd, yd;
-    laser_at_d(a.hp, a.clk_in->t + 0.5 * (double)a.dt, &xd, &yd, &s_beam[2]);
-    s_beam[0] = (float)xd;
-    s_beam[1] = (float)yd;
-    s_beam[3] = (float)(xd - (double)s_beam[0]);
-    s_beam[4] = (float)(yd - (double)s_beam[1]);
-  }
-  __syncthreads();
-  const float xl = s_beam[0], yl = s_beam[1], Pw = s_beam[2];
-  const DF xld{s_beam[0], s_beam[3]}, yld{s_beam[1], s_beam[4]};
-
   const int nx = a.nx, ny = a.ny, nz = a.nz;
+  // The beam enters only the top face: blocks whose z range ends below the
+  // top plane neither need it nor wait for its (float64) evaluation.
+  __shared__ float s_beam[5];  // xl, yl, P and the low parts of xl, yl
+  const bool top = min((int)(blockIdx.y + 1) * kHeatCompChunk, nz) == nz;  // block-uniform
+  if (top) {
+    if (threadIdx.x == 0) {
+      // the beam centre and power at mid-step, the centre also as double-float
+      double xd, yd;
+      laser_at_d(a.hp, a.clk_in->t + 0.5 * (double)a.dt, &xd, &yd, &s_beam[2]);
+      s_beam[0] = (float)xd;
+      s_beam[1] = (float)yd;
+      s_beam[3] = (float)(xd - (double)s_beam[0]);
+      s_beam[4] = (float)(yd - (double)s_beam[1]);
+    }
+    __syncthreads();
+  }
+  const float xl = top ? s_beam[0] : 0.f, yl = top ? s_beam[1] : 0.f;
+  const float Pw = top ? s_beam[2] : 0.f;
+  const DF xld{xl, top ? s_beam[3] : 0.f}, yld{yl, top ? s_beam[4] : 0.f};
+
   const int t = blockIdx.x * blockDim.x + threadIdx.x;  // host keeps nx * ny < 2^31
   const bool valid = t < nx * ny;
   // a spare lane shadows the last column (every lane takes part in the votes)

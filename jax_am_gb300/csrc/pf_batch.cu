@@ -207,7 +207,8 @@ extern "C" int pfg_batch_encode(const pfg_batch_job* jobs, int num_jobs, void* t
     if (J.params.num_oris % 4 == 0 &&
         plan_warp_tiles_ex(J.params.nx, J.params.ny, J.params.nz, J.params.num_oris, d.sm_count,
                            budget - 64, kThreads / 32, 0, 2 * kThreads, &t) &&
-        t.vec == 4 && t.stages <= kTmaMaxStages) {
+        t.vec == 4 && t.stages <= kTmaMaxStages &&
+        std::min(J.params.nz, 64) + 2 <= kTmaMaxPlanes) {
       t.rs = kThreads;
       tma = true;
     } else if (!plan_warp_tiles_ex(J.params.nx, J.params.ny, J.params.nz, J.params.num_oris,

@@ -14,6 +14,7 @@
 namespace pfg {
 
 constexpr int kTmaMaxStages = 8;  // ring slots of a batched unit, at most
+constexpr int kTmaMaxPlanes = 66;  // planes of a batched unit with its halo (z chunks <= 64)
 
 // Wait for the phase with this parity to complete; false (and *err set to
 // PFG_ERR_TIMEOUT) if the wait ran out.
@@ -170,6 +171,17 @@ __device__ __forceinline__ void tma_unit(const StepArgs& a, int unit, const floa
   }
   __syncthreads();
   const double t0 = s_t0;
+  // batched units (moving gradient): the temperature of each of the unit's
+  // planes, evaluated once (float64 arithmetic is slow on this GPU) rather
+  // than by every thread at every plane
+  __shared__ float s_Tq[kTmaMaxPlanes];
+  if constexpr (BATCH && TSRC == kTQuench) {
+    for (int j = threadIdx.x; j < nplanes; j += NC) {
+      const double zc = a.q.z_first + (double)(zb - 1 + j) * (double)a.h_z;
+      s_Tq[j] = (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t0);
+    }
+    __syncthreads();
+  }
   // the point source's record for this step (the same for every cell)
   pfg_point_source prec{};
   if constexpr (TSRC == kTPoint) prec = point_record(a.ps, s_step);
@@ -311,8 +323,13 @@ __device__ __forceinline__ void tma_unit(const StepArgs& a, int unit, const floa
     float4* cb = cc + (size_t)buf * P_ty * P_tx;
     TempCoef plane{};
     if constexpr (TSRC == kTQuench) {
-      const double zc = a.q.z_first + (double)pz * (double)a.h_z;
-      const float Tz = (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t0);
+      float Tz;
+      if constexpr (BATCH) {
+        Tz = s_Tq[pz - zb + 1];
+      } else {
+        const double zc = a.q.z_first + (double)pz * (double)a.h_z;
+        Tz = (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t0);
+      }
       plane = temp_coefficients_fast(a.pc, Tz, a.dt);
     }
 #pragma unroll
