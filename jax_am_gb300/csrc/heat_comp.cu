@@ -25,7 +25,7 @@ namespace pfg {
 
 constexpr int kHeatCompChunk = 8;  // cells marched per thread along z
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 heat_comp_kernel(const __grid_constant__ StepArgs a) {
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   // The beam enters only the top face: blocks whose z range ends below the

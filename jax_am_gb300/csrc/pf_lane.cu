@@ -43,6 +43,13 @@ __device__ __forceinline__ bool lane_wait(uint64_t* bar, unsigned parity,
   return false;
 }
 
+// The moving gradient's temperature of plane z at time t
+// (solidification/example.py:21-34), in float64 as the reference evaluates it.
+__device__ __forceinline__ float quench_T(const StepArgs& a, int z, double t) {
+  const double zc = a.q.z_first + (double)z * (double)a.h_z;
+  return (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t);
+}
+
 // Folded update of one element (allen_cahn.py:42-51,58,60-85 with the
 // Euler step, :106-114).  Per cell, k = (A1, B1, C1, W):
 //   eta' = e (A1 + B1 e^2) + (C1 + W (cn + cn^2)) lap'
@@ -147,6 +154,9 @@ __global__ void __launch_bounds__(NC, MINB) pf_lane_kernel(const __grid_constant
   __shared__ double s_t0;
   __shared__ long long s_step;
   __shared__ float s_beam[5];  // xl, yl, P and the low parts of xl, yl
+  // moving gradient: the temperature of plane z, evaluated by one thread a
+  // plane ahead (float64 arithmetic is slow on this GPU), double-buffered
+  __shared__ float s_Tq[2];
   __shared__ uint64_t s_never;  // a barrier nothing arrives on (the wait probe)
   if (threadIdx.x == 0) {
     s_abort = 0;
@@ -163,6 +173,7 @@ __global__ void __launch_bounds__(NC, MINB) pf_lane_kernel(const __grid_constant
       }
     }
     s_t0 = t;
+    if constexpr (TSRC == kTQuench) s_Tq[0] = quench_T(a, zb, t);
     s_step = (TSRC != kTArray) ? a.clk_in->step : 0;
     if constexpr (HEAT) {
       // beam centre and power at mid-step; the centre also as double-float
@@ -312,6 +323,9 @@ __global__ void __launch_bounds__(NC, MINB) pf_lane_kernel(const __grid_constant
       stage(m + S);
       issued = m + S + 1;
     }
+    // read in the next iteration, after its barrier
+    if constexpr (TSRC == kTQuench)
+      if (threadIdx.x == 0 && z + 1 < ze) s_Tq[(m + 1) & 1] = quench_T(a, z + 1, t0);
     const float* e1 = eta_s + s1 * SLOTF;
     const float* e2 = eta_s + s2 * SLOTF;
     load_cell<NV>(cc, e1 + own);
@@ -378,8 +392,7 @@ __global__ void __launch_bounds__(NC, MINB) pf_lane_kernel(const __grid_constant
         Tcell = Tnext;
         if (valid && z + 1 < ze) Tnext = __ldg(a.T + (int64_t)(z + 1) * plane_cells + cell0);
       } else if constexpr (TSRC == kTQuench) {
-        const double zc = a.q.z_first + (double)z * (double)a.h_z;
-        Tcell = (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t0);
+        Tcell = s_Tq[m & 1];
       } else if constexpr (TSRC == kTPoint) {
         Tcell = point_source_T(a.ps, prec, gx, gy, z);
       } else {  // kTInterp
