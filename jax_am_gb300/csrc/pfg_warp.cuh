@@ -171,9 +171,25 @@ __device__ __forceinline__ void warp_unit(const StepArgs& a, int unit, double t0
   const uint64_t magic_tx2 = div_magic(txv + 2);
   const uint64_t magic_txv = div_magic(txv);
 
-  // ---- beam at mid-step; point-source record of this step
-  float xl = 0.f, yl = 0.f, Pw = 0.f;
-  if constexpr (TSRC == kTHeat) laser_at(a.hp, t0 + 0.5 * (double)a.dt, &xl, &yl, &Pw);
+  // ---- beam at mid-step (float64, evaluated by one thread: float64
+  // arithmetic is slow on this GPU); point-source record of this step
+  __shared__ float s_beam_w[3];
+  // moving gradient: the temperature of plane pz in s_Tw[(pz - zb) & 1],
+  // evaluated by one thread a barrier ahead of its use
+  __shared__ float s_Tw[2];
+  auto quench_T = [&](int pz) {
+    const double zc = a.q.z_first + (double)pz * (double)a.h_z;
+    return (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t0);
+  };
+  if (threadIdx.x == 0) {
+    if constexpr (TSRC == kTHeat)
+      laser_at(a.hp, t0 + 0.5 * (double)a.dt, &s_beam_w[0], &s_beam_w[1], &s_beam_w[2]);
+    if constexpr (TSRC == kTQuench) {
+      s_Tw[0] = quench_T(zb);
+      s_Tw[1] = quench_T(zb + 1);
+    }
+  }
+  float xl = 0.f, yl = 0.f, Pw = 0.f;  // read after the prologue's barrier
   pfg_point_source prec{};
   if constexpr (TSRC == kTPoint) prec = point_record(a.ps, a.clk_in->step);
   float w_past = 0.f;
@@ -191,11 +207,7 @@ __device__ __forceinline__ void warp_unit(const StepArgs& a, int unit, double t0
     const float* ts = T_s + (size_t)slot * a.tslot;
     float4* cb = cc + (size_t)buf * a.ty * a.tx;
     TempCoef plane{};
-    if constexpr (TSRC == kTQuench) {
-      const double zc = a.q.z_first + (double)pz * (double)a.h_z;
-      const float Tz = (float)(a.q.T_base + a.q.grad * (zc - a.q.z0) - a.q.grad * a.q.vel * t0);
-      plane = temp_coefficients_fast(a.pc, Tz, a.dt);
-    }
+    if constexpr (TSRC == kTQuench) plane = temp_coefficients_fast(a.pc, s_Tw[(pz - zb) & 1], a.dt);
     for (int i = threadIdx.x; i < tyv * txv; i += kThreads) {
       const int r = fast_div(i, magic_txv), c = i - r * txv;
       const float* ce = es + (r + 1) * a.pitch + (c + 1) * n;
@@ -240,6 +252,11 @@ __device__ __forceinline__ void warp_unit(const StepArgs& a, int unit, double t0
   }
   cp_async_wait(S - 4);
   __syncthreads();
+  if constexpr (TSRC == kTHeat) {
+    xl = s_beam_w[0];
+    yl = s_beam_w[1];
+    Pw = s_beam_w[2];
+  }
   cell_coefs(1, 0, zb);  // plane zb sits in slot 1
 
   const int64_t plane_elems = (int64_t)a.ny * a.nx * n;
@@ -252,6 +269,9 @@ __device__ __forceinline__ void warp_unit(const StepArgs& a, int unit, double t0
       if (pz <= ze) stage((m + S - 1) % S, pz);
       cp_async_commit();
     }
+    // read by cell_coefs(z + 2) after the next barrier
+    if constexpr (TSRC == kTQuench)
+      if (threadIdx.x == 0 && z + 2 < ze) s_Tw[(m + 2) & 1] = quench_T(z + 2);
     const int s_prev = m % S, s_cur = (m + 1) % S, s_next = (m + 2) % S;
 
     // ---- per-cell work: heat update of plane z, coefficients of plane z+1
