@@ -219,7 +219,7 @@ struct HeatConsts {
 };
 
 __device__ __forceinline__ float heat_k(const HeatConsts& H, float T) {
-  return 0.0163f * fminf(fmaxf(T, 300.f), H.Tl) + 4.5847f;  // gamma.py:14
+  return fmaf(0.0163f, fminf(fmaxf(T, 300.f), H.Tl), 4.5847f);  // gamma.py:14
 }
 
 // Whether the latent heat enters cp (gamma.py:12,15): the liquid fraction
@@ -236,7 +236,9 @@ __device__ __forceinline__ bool heat_mushy(const HeatConsts& H, float T) {
 // evaluated at the face temperature Tf (gamma.py:23-34).
 __device__ __forceinline__ float heat_robin(const HeatConsts& H, float Tf) {
   const float t2 = Tf * Tf;
-  return H.h * (Tf - H.T0) + H.sb_eps * (t2 * t2 - H.T0_4);
+  // one explicit fused multiply-add: with a * b + c * d the compiler may fuse
+  // either product, and which one can depend on the surrounding code
+  return fmaf(H.h, Tf - H.T0, H.sb_eps * fmaf(t2, t2, -H.T0_4));
 }
 
 // Evaluate the beam position and power at time t from the tool path.
@@ -280,34 +282,38 @@ __device__ __forceinline__ void heat_faces(const HeatConsts& H, float Tc, float 
                                            float& Tzp, int gx, int gy, int gz, float xl,
                                            float yl, float P, float* Tg_out, IDX idx, IDX sx,
                                            IDX sy, IDX sz) {
+  // Every a * b + c expression below is written as an explicit fmaf: left
+  // to the compiler, which product it fuses can depend on the surrounding
+  // code (which operands are loop-invariant), and the kernels that call
+  // this promise identical results in either axis order.
   if (gx == 0) {
-    Txm = Tc - heat_robin(H, (Tc + Txm) * 0.5f) * rk * H.dx;
+    Txm = fmaf(-(heat_robin(H, (Tc + Txm) * 0.5f) * rk), H.dx, Tc);
     Tg_out[idx - sx] = Txm;
   }
   if (gx == H.nx - 1) {
-    Txp = Tc - heat_robin(H, (Tc + Txp) * 0.5f) * rk * H.dx;
+    Txp = fmaf(-(heat_robin(H, (Tc + Txp) * 0.5f) * rk), H.dx, Tc);
     Tg_out[idx + sx] = Txp;
   }
   if (gy == 0) {
-    Tym = Tc - heat_robin(H, (Tc + Tym) * 0.5f) * rk * H.dy;
+    Tym = fmaf(-(heat_robin(H, (Tc + Tym) * 0.5f) * rk), H.dy, Tc);
     Tg_out[idx - sy] = Tym;
   }
   if (gy == H.ny - 1) {
-    Typ = Tc - heat_robin(H, (Tc + Typ) * 0.5f) * rk * H.dy;
+    Typ = fmaf(-(heat_robin(H, (Tc + Typ) * 0.5f) * rk), H.dy, Tc);
     Tg_out[idx + sy] = Typ;
   }
   if (gz == 0) {
-    Tzm = Tc - heat_robin(H, (Tc + Tzm) * 0.5f) * rk * H.dz;
+    Tzm = fmaf(-(heat_robin(H, (Tc + Tzm) * 0.5f) * rk), H.dz, Tc);
     Tg_out[idx - sz] = Tzm;
   }
   if (gz == H.nz - 1) {
     // top face: convection + radiation minus the Gaussian beam flux (gamma.py:33-35)
-    const float x = H.x_first + (float)gx * H.dx;
-    const float y = H.y_first + (float)gy * H.dy;
+    const float x = fmaf((float)gx, H.dx, H.x_first);
+    const float y = fmaf((float)gy, H.dy, H.y_first);
     const float ddx = x - xl, ddy = y - yl;
-    const float beam = P * H.beam_coef * expf(-(ddx * ddx + ddy * ddy) * H.two_over_r2);
-    const float q = heat_robin(H, (Tc + Tzp) * 0.5f) - beam;
-    Tzp = Tc - q * rk * H.dz;
+    const float e = expf(-fmaf(ddx, ddx, ddy * ddy) * H.two_over_r2);
+    const float q = fmaf(-(P * H.beam_coef), e, heat_robin(H, (Tc + Tzp) * 0.5f));
+    Tzp = fmaf(-(q * rk), H.dz, Tc);
     Tg_out[idx + sz] = Tzp;
   }
 }
@@ -326,15 +332,17 @@ __device__ __forceinline__ float heat_cell_update(const HeatConsts& H, float Tc,
                                                   float yl, float P, float dt, float* Tg_out,
                                                   IDX idx, IDX sx, IDX sy, IDX sz) {
   const float k = heat_k(H, Tc);
-  const float cp = 0.2441f * fminf(fmaxf(Tc, 300.f), H.Tl) + 338.39f +
+  const float cp = fmaf(0.2441f, fminf(fmaxf(Tc, 300.f), H.Tl), 338.39f) +
                    (heat_mushy(H, Tc) ? H.latent : 0.f);  // gamma.py:12-15
   if constexpr (FACES)
     heat_faces(H, Tc, rcp_approx(k), Txm, Txp, Tym, Typ, Tzm, Tzp, gx, gy, gz, xl, yl, P, Tg_out,
                idx, sx, sy, sz);
-  const float txx = (Txm - 2.f * Tc + Txp) * H.rdx2;  // gamma.py:49-51
-  const float tyy = (Tym - 2.f * Tc + Typ) * H.rdy2;
-  const float tzz = (Tzm - 2.f * Tc + Tzp) * H.rdz2;
-  return Tc + dt * ((k * H.inv_rho) * rcp_approx(cp) * (txx + tyy + tzz));
+  // gamma.py:49-51, with explicit fused multiply-adds (see heat_faces)
+  const float ax = fmaf(-2.f, Tc, Txm) + Txp;
+  const float ay = fmaf(-2.f, Tc, Tym) + Typ;
+  const float az = fmaf(-2.f, Tc, Tzm) + Tzp;
+  const float lap = fmaf(ax, H.rdx2, fmaf(ay, H.rdy2, az * H.rdz2));
+  return fmaf(dt, (k * H.inv_rho) * rcp_approx(cp) * lap, Tc);
 }
 
 // ---------------------------------------------------------------------------
@@ -445,7 +453,7 @@ __device__ __forceinline__ DF heat_update_df_near_ambient(const HeatConsts& H, D
                                                          float* Th_out, float* Tl_out, int idx,
                                                          int sx, int sy, int sz) {
   const float k = heat_k(H, Tc.h);
-  const float cp = 0.2441f * fminf(fmaxf(Tc.h, 300.f), H.Tl) + 338.39f +
+  const float cp = fmaf(0.2441f, fminf(fmaxf(Tc.h, 300.f), H.Tl), 338.39f) +
                    (heat_mushy(H, Tc.h) ? H.latent : 0.f);
   if constexpr (FACES) {
     const float rk = rcp_approx(k);
@@ -457,10 +465,10 @@ __device__ __forceinline__ DF heat_update_df_near_ambient(const HeatConsts& H, D
       if (!on[f]) continue;
       float q = heat_robin(H, (Tc.h + n[f].h) * 0.5f);
       if (f == 5) {
-        const float x = H.x_first + (float)gx * H.dx;
-        const float y = H.y_first + (float)gy * H.dy;
+        const float x = fmaf((float)gx, H.dx, H.x_first);
+        const float y = fmaf((float)gy, H.dy, H.y_first);
         const float ddx = x - xl, ddy = y - yl;
-        q -= P * H.beam_coef * expf(-(ddx * ddx + ddy * ddy) * H.two_over_r2);
+        q = fmaf(-(P * H.beam_coef), expf(-fmaf(ddx, ddx, ddy * ddy) * H.two_over_r2), q);
       }
       const DF g = df_add_f(Tc, -q * rk * d[f >> 1]);
       Th_out[fidx[f]] = g.h;
