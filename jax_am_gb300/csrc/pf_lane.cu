@@ -250,9 +250,14 @@ __global__ void __launch_bounds__(NC, MINB) pf_lane_kernel(const __grid_constant
   };
 
   // ---- this thread's cell
-  const int tr = threadIdx.x / TX, tc = threadIdx.x % TX;
+  // a warp owns an 8 x 4 block of cells (rows of 8 lanes): its cells and
+  // their neighbours span fewer grains than a 16 x 2 strip, so more of its
+  // orientation vectors are exact zeros (1.4 % faster than 16 x 2); a row of
+  // 8 lanes at an 80-byte stride reads shared memory without bank conflicts
+  const int tr = ((threadIdx.x >> 5) / (TX / 8)) * 4 + ((threadIdx.x & 31) >> 3);
+  const int tc = ((threadIdx.x >> 5) % (TX / 8)) * 8 + (threadIdx.x & 7);
   const bool valid = tr < tyv && tc < txv;
-  const bool warp_on = (threadIdx.x & ~31) / TX < tyv;  // some row of this warp is in the tile
+  const bool warp_on = ((threadIdx.x >> 5) / (TX / 8)) * 4 < tyv;  // some row of this warp is in the tile
   const int gx = x0 + tc, gy = y0 + tr;
   const int own = (tr + 1) * ROWF + (tc + 1) * N;  // staged offset of the cell
   // Neumann along x: the edge cell is its own neighbour (its halo is not staged)
