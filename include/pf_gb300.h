@@ -223,7 +223,9 @@ int pfg_tune(int key, int value);
  * device, as 12 int32: kernel, VEC, lanes per
  * cell, tile x, tile y, warps along x, rows per warp, plane slots, planes per
  * unit, CTAs, dynamic shared memory bytes, SM count.  kernel: 1 generic,
- * 2 cp.async warp-per-cells, 3 TMA-fed. */
+ * 2 cp.async warp-per-cells, 3 TMA-fed, 4 cell-per-lane (one cell per
+ * lane: a warp owns 8 x 4 cells, so warps along x = tile x / 8 and rows per
+ * warp = 4). */
 int pfg_describe_plan(const pfg_pf_params* p, int32_t* out);
 
 /* Which compile-time tile plan the TMA-fed kernel runs for these parameters

@@ -514,9 +514,9 @@ bool plan_lane_tiles(int nx, int ny, int nz, int n, int sm_count, int max_smem_p
   t.tpc = 1;
   t.tx = tx;
   t.ty = ty;
-  t.cpw = 32;
-  t.wx = 1;
-  t.rpw = 32 / tx;
+  t.cpw = 8;        // a warp owns 8 x 4 cells
+  t.wx = tx / 8;
+  t.rpw = 4;
   t.rs = kLaneNC;
   t.stages = S;
   t.pitch = (tx + 2) * n;
