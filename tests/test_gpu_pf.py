@@ -262,6 +262,9 @@ def test_plans_report_the_kernel_used():
         poly, eta, T, pf_args, _, _ = pf_case(shape, n, 0.15, seed=n, bc=bc)
         plan = _lib.describe_plan(make_pf_params(pf_args, poly))
         assert plan["kernel"] == kernel and plan["vec"] == vec, (shape, n, bc, plan)
+        if kernel == 4:  # cell per lane: 16 x 16 tiles, a warp owns 8 x 4 cells
+            assert (plan["tile_x"], plan["tile_y"], plan["warps_x"], plan["rows_per_warp"],
+                    plan["lanes_per_cell"]) == (16, 16, 2, 4, 1), plan
     lib.pfg_set_kernel_variant(1)
     assert _lib.describe_plan(make_pf_params(pf_args, poly))["kernel"] == 1
     poly, eta, T, pf_args, _, _ = pf_case((30, 20, 10), 20, 0.15, seed=20)
