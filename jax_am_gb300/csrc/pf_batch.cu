@@ -6,8 +6,13 @@
 // arguments (grid, tile plan, physics, grain directions), its double buffer,
 // start time and step counters, and the prefix sum of work units.  A fixed
 // grid of persistent CTAs (two per SM) walks the units of all jobs; each unit
-// is a tile x z-chunk of one job, processed by the same warp-per-cells body as
-// the single-job kernel.  Because the grid and the table's address never
+// is a tile x z-chunk of one job, processed by the single-job kernels' unit
+// bodies: the TMA-fed body (pfg_tma.cuh) for orientation counts that are a
+// multiple of 4 (the server pads every job to one), else the cp.async
+// warp-per-cells body (pfg_warp.cuh).  A unit's job arguments are copied to
+// shared memory, and the TMA-fed body's ring barriers, in static shared
+// memory, are invalidated and initialised again for every unit.  Because the
+// grid and the table's address never
 // change, a graph of K launches (k = 0 .. K-1) is captured once and replayed
 // while the host rewrites the table between replays (admitting and retiring
 // jobs: continuous batching).
